@@ -1,0 +1,312 @@
+"""Benchmark: exact Q(N) row-boundary contraction at N=18 on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 18]
+
+One step = one complete exact contraction of Q(N) (all rows, all first-row
+orbit slices) through the library's C ABI. Prints one JSON line.
+
+value  : boundary entries per second = (sum over row steps of boundary
+         entries read by the merge) / (device time of the whole contraction,
+         CUDA events on the library's stream).
+e2e    : the same entries / wall time of the C-ABI call (host seeding,
+         host->device upload of the seed boundary, all row steps, device->host
+         read-back of every row's metrics and of the count residues).
+roofline: the merge step (expand-insert + compact kernels), algorithmic bytes
+         E*(S_in+S_out) per step over the kernels' CUDA-event time.
+cpu_baseline: the CPU oracle (threaded restatement of the reference's
+         sort-reduce driver) on the first rows of the same workload.
+
+--impl reference times only that CPU restatement (there is no runnable
+reference binary: the reference is Rust and no Rust toolchain exists here).
+Inputs are synthetic by construction: the workload is the empty N x N board.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+PACKAGE = "quantum-harness-peps-naive_gb300"
+METRIC = "Q(N) wall time & boundary entries/s at N=18 (bit-exact)"
+UNIT = "boundary entries/s"
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def cpu_sample(n: int, rows: int, threads: int):
+    """Oracle (threaded sort-reduce restatement) on the first `rows` rows."""
+    import oracle_py  # noqa: PLC0415
+
+    oracle_py.build()
+    t0 = time.perf_counter()
+    r = oracle_py.contract(n, backend=oracle_py.PARALLEL_SORT_REDUCE, threads=threads, rows=rows)
+    wall = time.perf_counter() - t0
+    entries = sum(l["input_states"] for l in r["layers"])
+    return entries, wall, r
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(args.n, args.cpu_rows, threads)
+    vals, walls, entries = [], [], 0
+    for _ in range(args.steps):
+        e, w, _ = cpu_sample(args.n, args.cpu_rows, threads)
+        vals.append(e / w)
+        walls.append(w)
+        entries = e
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": statistics.median(walls) * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64 keys + u128 checked coefficients",
+        "data": "synthetic (empty N x N board)",
+        "config": {"workload": f"Q({args.n}) orbit-sliced row contraction, first {args.cpu_rows} rows",
+                   "n": args.n, "rows": args.cpu_rows},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"first {args.cpu_rows} rows of Q({args.n}) ({entries} boundary entries), "
+                                   f"threaded C++ restatement of contract_rows_d4_orbit_parallel_sort_reduce"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    world, rank, local = dist_env()
+    pkg = importlib.import_module(PACKAGE)
+    if not pkg.LIBRARY_PATH.exists():
+        pkg.build()
+    if world > 1:
+        import torch  # noqa: PLC0415
+        import torch.distributed as dist  # noqa: PLC0415
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    ctx = pkg.Context(local if world > 1 else 0)
+    opts = {}
+    if args.slice_depth:
+        opts["slice_depth"] = args.slice_depth
+    if args.grain == "site":
+        opts["granularity"] = pkg.GRAIN_SITE
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist  # noqa: PLC0415
+
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        r = ctx.contract_rows(args.n, **opts)
+        assert r.count == pkg.known_count(args.n)
+    barrier()
+    sampler = ClockSampler(local if world > 1 else 0)
+    sampler.start()
+    results, walls = [], []
+    t_all0 = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = ctx.contract_rows(args.n, **opts)
+        walls.append(time.perf_counter() - t0)
+        if r.count != pkg.known_count(args.n):
+            raise SystemExit(f"count mismatch: {r.count} != {pkg.known_count(args.n)}")
+        results.append(r)
+    t_all = time.perf_counter() - t_all0
+    barrier()
+    clocks = sampler.stop()
+
+    entries = results[-1].device["entries_in"]
+    dev_s = max(sum(x.device["device_ms"] for x in results) / len(results) / 1e3, 1e-12)
+    wall_s = max(t_all / args.steps, 1e-12)
+    if world > 1:
+        import torch  # noqa: PLC0415
+        import torch.distributed as dist  # noqa: PLC0415
+
+        t = torch.tensor([dev_s, wall_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall_s = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    value = entries * world / dev_s
+    e2e = entries * world / wall_s
+
+    peak, peak_kind = measured_peaks()
+    d = results[-1].device
+    merge_s = d["merge_kernel_ms"] / 1e3 if d["merge_kernel_ms"] else 0.0
+    achieved = d["merge_kernel_bytes"] / max(d["device_ms"] / 1e3, 1e-12) / 1e9
+    roofline = {
+        "bound": "hbm",
+        "kernel": "merge step: row_expand_insert_kernel + compact_kernel (hash merge)",
+        "achieved": achieved,
+        "peak": peak,
+        "peak_kind": peak_kind,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": None,
+        "algorithmic_bytes_per_step": d["merge_kernel_bytes"],
+        "launches_per_step": d["merge_kernel_launches"],
+        "expand_insert_ms_per_step": d["merge_kernel_ms"],
+        "merge_ms_per_step": d["device_ms"],
+    }
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wall_s * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": f"u{d['key_bits']} keys + {d['residues']}x u32 residues",
+        "data": "synthetic (empty N x N board; the workload has no external input)",
+        "config": {
+            "workload": f"Q({args.n}) exact, all first-row orbit slices",
+            "n": args.n,
+            "grain": args.grain,
+            "slice_depth": d["slice_depth"],
+            "batches": d["batches"],
+            "residues": d["residues"],
+            "key_bits": d["key_bits"],
+            "l2": "inputs larger than L2 (boundary buffers of GBs per row)",
+            "parallelism": "replicas" if world > 1 else "single",
+        },
+        "count": str(results[-1].count),
+        "wall_s_per_step": wall_s,
+        "device_s_per_step": dev_s,
+        "boundary_entries_per_step": entries,
+        "peak_states": results[-1].peak_states,
+        "peak_device_bytes": d["peak_device_bytes"],
+        "gpu_launches": sum(x.device["gpu_launches"] for x in results),
+        "clocks": clocks,
+        "roofline": roofline,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        ce, cw, _ = cpu_sample(args.n, args.cpu_rows, threads)
+        line["cpu_baseline"] = {
+            "value": ce / cw, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {args.cpu_rows} rows of Q({args.n}) ({ce} boundary entries), threaded C++ "
+                      f"restatement of contract_rows_d4_orbit_parallel_sort_reduce",
+        }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=18)
+    ap.add_argument("--grain", choices=["row", "site"], default="row")
+    ap.add_argument("--slice-depth", type=int, default=0)
+    ap.add_argument("--cpu-rows", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * qpeps.h — C ABI of the GB300 exact N-Queens PEPS row-boundary contraction.
+ *
+ * Plain C types only (fixed-width integers, pointers, sizes); no CUDA or
+ * C++ types cross this boundary, so a Rust `extern "C"` block, Python ctypes
+ * or a C program can bind it directly.
+ *
+ * Each entry point names the reference interface it replaces (Rust crate
+ * `nqueens-peps-naive`, file:line within that project).
+ *
+ * Ownership: the caller owns every output buffer; the library owns device
+ * memory behind an opaque `qpeps_ctx`. Threading: one context is used by one
+ * thread at a time; separate contexts may run concurrently (each owns one CUDA
+ * stream). Errors: every fallible call returns 0 on success or a QPEPS_ERR_*
+ * code, and writes a NUL-terminated message into `err` (when non-NULL)
+ * phrased like the reference's `Err(String)` values.
+ */
+#ifndef QPEPS_H
+#define QPEPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QPEPS_ABI_VERSION 1
+
+/* Return codes. */
+#define QPEPS_OK 0
+#define QPEPS_ERR_RANGE 1     /* N out of range, key too wide, bad prefix column */
+#define QPEPS_ERR_OOM 2       /* device or host allocation failed */
+#define QPEPS_ERR_CAPACITY 3  /* a device table or probe bound was exceeded */
+#define QPEPS_ERR_CRT_BOUND 4 /* reconstructed count fails the N! certificate */
+#define QPEPS_ERR_CUDA 5      /* CUDA runtime error */
+#define QPEPS_ERR_INVALID 6   /* invalid argument, or C failed certification */
+#define QPEPS_ERR_OVERFLOW 7  /* checked u128 arithmetic overflowed */
+#define QPEPS_ERR_TIMEOUT 8   /* a bounded device wait gave up */
+
+/* u128 as two little-endian u64 halves (Rust u128 / C unsigned __int128). */
+typedef struct qpeps_u128 {
+  uint64_t lo;
+  uint64_t hi;
+} qpeps_u128;
+
+/* Per-row metrics; field-for-field the reference's LayerMetric
+ * (src/lib.rs:388-401). `row` is 0-based like the reference (the CLI prints
+ * row+1). `peak_rss_bytes` reports device bytes in use by the context. */
+typedef struct qpeps_layer {
+  uint32_t row;
+  uint64_t input_states;
+  qpeps_u128 tensor_entries_examined;
+  qpeps_u128 tensor_entries_matched;
+  qpeps_u128 row_operator_candidates;
+  qpeps_u128 row_operator_matched;
+  qpeps_u128 completed_row_terms;
+  uint64_t output_states;
+  qpeps_u128 output_weight;
+  double elapsed_s;
+  uint64_t peak_rss_bytes;
+} qpeps_layer;
+
+/* Whole-contraction result; the reference's ContractionResult
+ * (src/lib.rs:403-415) plus device-side facts. */
+typedef struct qpeps_result {
+  uint32_t n;
+  qpeps_u128 count;
+  double elapsed_s;
+  uint64_t peak_states;
+  qpeps_u128 tensor_entries_examined;
+  qpeps_u128 tensor_entries_matched;
+  qpeps_u128 row_operator_candidates;
+  qpeps_u128 row_operator_matched;
+  uint64_t peak_rss_bytes;
+  uint32_t n_layers;
+  /* device-side facts (no reference counterpart) */
+  uint32_t residues;          /* CRT primes used */
+  uint32_t key_bits;          /* 64 or 128 */
+  uint32_t slice_depth;       /* rows enumerated on the host into slices */
+  uint32_t batches;           /* device batches run */
+  uint32_t merge;             /* merge strategy actually used (QPEPS_MERGE_*) */
+  uint64_t entries_in;        /* sum over row steps of boundary entries read */
+  uint64_t entries_out;       /* sum over row steps of boundary entries written */
+  uint64_t candidates;        /* sum over row steps of successor terms */
+  uint64_t gpu_launches;      /* kernels launched by this call */
+  uint64_t peak_device_bytes; /* high-water mark of the context's device pool */
+  double device_ms;           /* device time of all row steps (CUDA events) */
+  double merge_kernel_ms;     /* device time of the dominant merge kernel */
+  uint64_t merge_kernel_launches;
+  uint64_t merge_kernel_bytes; /* algorithmic bytes of the dominant kernel */
+  uint32_t residue_primes[4];
+  uint64_t count_residues[4];
+} qpeps_result;
+
+#define QPEPS_GRAIN_ROW 0  /* compiled row operator, one fused step per row */
+#define QPEPS_GRAIN_SITE 1 /* explicit C, one plain launch per site */
+
+#define QPEPS_MERGE_AUTO 0
+#define QPEPS_MERGE_HASH 1      /* global open-addressing table */
+#define QPEPS_MERGE_PARTITION 2 /* radix partition + shared-memory merge */
+
+typedef struct qpeps_options {
+  uint32_t struct_size;          /* sizeof(qpeps_options) */
+  uint32_t granularity;          /* QPEPS_GRAIN_* */
+  uint32_t merge;                /* QPEPS_MERGE_* */
+  uint32_t residues;             /* 0 = shortest prime prefix with product > N!, else 1..4 */
+  uint32_t key_bits;             /* 0 = narrowest that fits, 64 or 128 to force */
+  uint32_t slice_depth;          /* 0 = auto, else rows enumerated on the host (>= 1) */
+  uint32_t symmetry;             /* 1 = first-row vertical-reflection orbits (reference default) */
+  uint32_t collect_layers;       /* 1 = fill per-row metrics */
+  uint32_t block_threads;        /* 0 = auto */
+  uint32_t use_graph;            /* 1 = replay row steps through captured CUDA graphs */
+  uint64_t device_budget_bytes;  /* 0 = auto (a fraction of free device memory) */
+} qpeps_options;
+
+/* Library version string, e.g. "qpeps-gb300 0.1.0 (sm_103a)". */
+const char* qpeps_version(void);
+
+/* Fill `opt` with the defaults (reference semantics: row grain, orbits on). */
+void qpeps_options_default(qpeps_options* opt);
+
+/* Replaces `known_count` (src/lib.rs:5752-5784): Q(0..27). Returns
+ * QPEPS_ERR_RANGE for N > 27. */
+int qpeps_known_count(uint32_t n, qpeps_u128* out);
+
+/* Create / destroy a context bound to one CUDA device. */
+int qpeps_ctx_create(int device, void** ctx_out, char* err, size_t err_len);
+void qpeps_ctx_destroy(void* ctx);
+
+/* Replaces `contract_rows(n)` (src/lib.rs:758, via
+ * contract_rows_d4_orbit_sort_reduce 784 and
+ * contract_rows_sort_reduce_with_modes 5287-5415): exact count of Q(N) with
+ * per-row metrics. `layers` may be NULL; otherwise it receives up to
+ * `layers_cap` rows. N > 42 -> QPEPS_ERR_RANGE with the reference's message;
+ * N = 0 -> count 1. */
+int qpeps_contract_rows(void* ctx, uint32_t n, const qpeps_options* opt, qpeps_result* result,
+                        qpeps_layer* layers, uint32_t layers_cap, char* err, size_t err_len);
+
+/* Count completions of one board with `k` rows already placed (`prefix[r]`
+ * is the queen's column in row r; NULL when k = 0). k = 0 equals
+ * contract_rows(n).count. An attacked prefix gives 0. This has no single
+ * reference function: it is the prefix boundary of
+ * recursive_tail_successor (src/lib.rs:3139-3151) contracted like
+ * contract_rows. */
+int qpeps_count(void* ctx, uint32_t n, const uint32_t* prefix, uint32_t k, const qpeps_options* opt,
+                qpeps_u128* count_out, qpeps_result* stats_out, char* err, size_t err_len);
+
+/* Many independent instances in one call: instance i has board size n[i]
+ * and k[i] placed rows stored at prefix_cols[prefix_offset[i] ...]. Results
+ * go to counts[i]. Instances share device batches. */
+int qpeps_count_batch(void* ctx, uint32_t num, const uint32_t* n, const uint32_t* k,
+                      const uint32_t* prefix_offset, const uint32_t* prefix_cols,
+                      const qpeps_options* opt, qpeps_u128* counts, char* err, size_t err_len);
+
+/* Certification of the local tensor: run the equivalent of
+ * CompiledRowOperator::compile (src/lib.rs:430-485) on C given as
+ * `len` entries of (legs_key, value) where legs_key follows
+ * src/lib.rs:159-168. Returns 0 when C is exactly the Sec. VI automaton. The
+ * device kernels are only launched after this check passes on the library's
+ * own C. */
+int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QPEPS_H */

@@ -1,0 +1,398 @@
+"""GB300 exact N-Queens PEPS row-boundary contraction: Python mirror of the
+reference library API over the C ABI in include/qpeps.h.
+
+Reference (Rust crate ``nqueens-peps-naive``):
+
+* ``contract_rows(n) -> Result<ContractionResult, String>``  src/lib.rs:758
+* ``known_count(n) -> Option<u128>``                          src/lib.rs:5752-5784
+* ``ContractionResult`` / ``LayerMetric``                     src/lib.rs:388-415
+
+``contract_rows`` returns the same fields with the same meaning and raises
+``ContractionError`` where the reference returns ``Err(String)`` (same
+message text, e.g. N > 42). The device library must be built
+(``build.py``); there is no CPU fallback: importing the module on a machine
+without the library or without a CUDA device raises when a context is
+needed.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import threading
+from pathlib import Path
+from typing import Iterable, Sequence
+
+_PKG = Path(__file__).resolve().parent
+LIBRARY_PATH = _PKG / "libqpeps.so"
+
+QPEPS_OK = 0
+QPEPS_ERR_RANGE = 1
+QPEPS_ERR_OOM = 2
+QPEPS_ERR_CAPACITY = 3
+QPEPS_ERR_CRT_BOUND = 4
+QPEPS_ERR_CUDA = 5
+QPEPS_ERR_INVALID = 6
+QPEPS_ERR_OVERFLOW = 7
+QPEPS_ERR_TIMEOUT = 8
+
+GRAIN_ROW = 0
+GRAIN_SITE = 1
+MERGE_AUTO = 0
+MERGE_HASH = 1
+MERGE_PARTITION = 2
+
+
+class U128(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_uint64), ("hi", ctypes.c_uint64)]
+
+    @property
+    def value(self) -> int:
+        return (int(self.hi) << 64) | int(self.lo)
+
+
+class Layer(ctypes.Structure):
+    _fields_ = [
+        ("row", ctypes.c_uint32),
+        ("input_states", ctypes.c_uint64),
+        ("tensor_entries_examined", U128),
+        ("tensor_entries_matched", U128),
+        ("row_operator_candidates", U128),
+        ("row_operator_matched", U128),
+        ("completed_row_terms", U128),
+        ("output_states", ctypes.c_uint64),
+        ("output_weight", U128),
+        ("elapsed_s", ctypes.c_double),
+        ("peak_rss_bytes", ctypes.c_uint64),
+    ]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint32),
+        ("count", U128),
+        ("elapsed_s", ctypes.c_double),
+        ("peak_states", ctypes.c_uint64),
+        ("tensor_entries_examined", U128),
+        ("tensor_entries_matched", U128),
+        ("row_operator_candidates", U128),
+        ("row_operator_matched", U128),
+        ("peak_rss_bytes", ctypes.c_uint64),
+        ("n_layers", ctypes.c_uint32),
+        ("residues", ctypes.c_uint32),
+        ("key_bits", ctypes.c_uint32),
+        ("slice_depth", ctypes.c_uint32),
+        ("batches", ctypes.c_uint32),
+        ("merge", ctypes.c_uint32),
+        ("entries_in", ctypes.c_uint64),
+        ("entries_out", ctypes.c_uint64),
+        ("candidates", ctypes.c_uint64),
+        ("gpu_launches", ctypes.c_uint64),
+        ("peak_device_bytes", ctypes.c_uint64),
+        ("device_ms", ctypes.c_double),
+        ("merge_kernel_ms", ctypes.c_double),
+        ("merge_kernel_launches", ctypes.c_uint64),
+        ("merge_kernel_bytes", ctypes.c_uint64),
+        ("residue_primes", ctypes.c_uint32 * 4),
+        ("count_residues", ctypes.c_uint64 * 4),
+    ]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("granularity", ctypes.c_uint32),
+        ("merge", ctypes.c_uint32),
+        ("residues", ctypes.c_uint32),
+        ("key_bits", ctypes.c_uint32),
+        ("slice_depth", ctypes.c_uint32),
+        ("symmetry", ctypes.c_uint32),
+        ("collect_layers", ctypes.c_uint32),
+        ("block_threads", ctypes.c_uint32),
+        ("use_graph", ctypes.c_uint32),
+        ("device_budget_bytes", ctypes.c_uint64),
+    ]
+
+
+# Every symbol include/qpeps.h declares, with its ctypes signature.
+_VP = ctypes.c_void_p
+_SIGNATURES = {
+    "qpeps_version": (ctypes.c_char_p, []),
+    "qpeps_options_default": (None, [ctypes.POINTER(Options)]),
+    "qpeps_known_count": (ctypes.c_int, [ctypes.c_uint32, ctypes.POINTER(U128)]),
+    "qpeps_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_VP), ctypes.c_char_p, ctypes.c_size_t]),
+    "qpeps_ctx_destroy": (None, [_VP]),
+    "qpeps_contract_rows": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.POINTER(Options), ctypes.POINTER(Result), ctypes.POINTER(Layer),
+         ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "qpeps_count": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.POINTER(Options),
+         ctypes.POINTER(U128), ctypes.POINTER(Result), ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "qpeps_count_batch": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+         ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(Options),
+         ctypes.POINTER(U128), ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "qpeps_certify_c": (
+        ctypes.c_int,
+        [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_char_p,
+         ctypes.c_size_t],
+    ),
+}
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def library() -> ctypes.CDLL:
+    """Load libqpeps.so (raises if it has not been built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not LIBRARY_PATH.exists():
+                raise ContractionError(QPEPS_ERR_CUDA, f"device library not built: {LIBRARY_PATH}")
+            lib = ctypes.CDLL(str(LIBRARY_PATH))
+            for name, (res, args) in _SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+        return _lib
+
+
+class ContractionError(RuntimeError):
+    """The reference's ``Err(String)``; ``code`` is the QPEPS_ERR_* value."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+        self.message = message
+
+
+def _check(rc: int, err: ctypes.Array) -> None:
+    if rc != QPEPS_OK:
+        raise ContractionError(rc, err.value.decode(errors="replace"))
+
+
+@dataclasses.dataclass
+class LayerMetric:
+    """src/lib.rs:388-401 (``row`` is 0-based)."""
+
+    row: int
+    input_states: int
+    tensor_entries_examined: int
+    tensor_entries_matched: int
+    row_operator_candidates: int
+    row_operator_matched: int
+    completed_row_terms: int
+    output_states: int
+    output_weight: int
+    elapsed: float
+    peak_rss_bytes: int
+
+
+@dataclasses.dataclass
+class ContractionResult:
+    """src/lib.rs:403-415 plus device-side facts in ``device``."""
+
+    n: int
+    count: int
+    elapsed: float
+    peak_states: int
+    tensor_entries_examined: int
+    tensor_entries_matched: int
+    row_operator_candidates: int
+    row_operator_matched: int
+    peak_rss_bytes: int
+    layers: list
+    device: dict
+
+
+def options(**kw) -> Options:
+    """Options with the library defaults, overridden by keyword."""
+    o = Options()
+    library().qpeps_options_default(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k) or k == "struct_size":
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, int(v))
+    return o
+
+
+def _result_from(res: Result, layers: Sequence[Layer] | None) -> ContractionResult:
+    lay = []
+    if layers is not None:
+        for i in range(min(res.n_layers, len(layers))):
+            L = layers[i]
+            lay.append(
+                LayerMetric(
+                    row=L.row,
+                    input_states=L.input_states,
+                    tensor_entries_examined=L.tensor_entries_examined.value,
+                    tensor_entries_matched=L.tensor_entries_matched.value,
+                    row_operator_candidates=L.row_operator_candidates.value,
+                    row_operator_matched=L.row_operator_matched.value,
+                    completed_row_terms=L.completed_row_terms.value,
+                    output_states=L.output_states,
+                    output_weight=L.output_weight.value,
+                    elapsed=L.elapsed_s,
+                    peak_rss_bytes=L.peak_rss_bytes,
+                )
+            )
+    device = {
+        "residues": res.residues,
+        "key_bits": res.key_bits,
+        "slice_depth": res.slice_depth,
+        "batches": res.batches,
+        "merge": res.merge,
+        "entries_in": res.entries_in,
+        "entries_out": res.entries_out,
+        "candidates": res.candidates,
+        "gpu_launches": res.gpu_launches,
+        "peak_device_bytes": res.peak_device_bytes,
+        "device_ms": res.device_ms,
+        "merge_kernel_ms": res.merge_kernel_ms,
+        "merge_kernel_launches": res.merge_kernel_launches,
+        "merge_kernel_bytes": res.merge_kernel_bytes,
+        "residue_primes": list(res.residue_primes)[: res.residues],
+        "count_residues": list(res.count_residues)[: res.residues],
+    }
+    return ContractionResult(
+        n=res.n,
+        count=res.count.value,
+        elapsed=res.elapsed_s,
+        peak_states=res.peak_states,
+        tensor_entries_examined=res.tensor_entries_examined.value,
+        tensor_entries_matched=res.tensor_entries_matched.value,
+        row_operator_candidates=res.row_operator_candidates.value,
+        row_operator_matched=res.row_operator_matched.value,
+        peak_rss_bytes=res.peak_rss_bytes,
+        layers=lay,
+        device=device,
+    )
+
+
+class Context:
+    """One CUDA device and its device-memory pool (``qpeps_ctx``)."""
+
+    def __init__(self, device: int = 0):
+        lib = library()
+        err = ctypes.create_string_buffer(512)
+        h = _VP()
+        _check(lib.qpeps_ctx_create(device, ctypes.byref(h), err, len(err)), err)
+        self._h = h
+        self._lock = threading.Lock()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            library().qpeps_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def contract_rows(self, n: int, **opts) -> ContractionResult:
+        """Replaces ``contract_rows(n)`` (src/lib.rs:758)."""
+        lib = library()
+        o = options(**opts)
+        res = Result()
+        cap = max(int(n), 1)
+        layers = (Layer * cap)()
+        err = ctypes.create_string_buffer(512)
+        with self._lock:
+            rc = lib.qpeps_contract_rows(self._h, int(n), ctypes.byref(o), ctypes.byref(res), layers, cap, err, len(err))
+        _check(rc, err)
+        return _result_from(res, layers)
+
+    def count(self, n: int, prefix: Sequence[int] = (), **opts) -> int:
+        """Completions of a board with ``len(prefix)`` rows placed."""
+        c, _ = self.count_with_stats(n, prefix, **opts)
+        return c
+
+    def count_with_stats(self, n: int, prefix: Sequence[int] = (), **opts):
+        lib = library()
+        o = options(**opts)
+        k = len(prefix)
+        arr = (ctypes.c_uint32 * max(k, 1))(*prefix)
+        out = U128()
+        res = Result()
+        err = ctypes.create_string_buffer(512)
+        with self._lock:
+            rc = lib.qpeps_count(self._h, int(n), arr if k else None, k, ctypes.byref(o), ctypes.byref(out),
+                                 ctypes.byref(res), err, len(err))
+        _check(rc, err)
+        return out.value, _result_from(res, None)
+
+    def count_batch(self, instances: Iterable[tuple[int, Sequence[int]]], **opts) -> list[int]:
+        lib = library()
+        inst = list(instances)
+        num = len(inst)
+        ns = (ctypes.c_uint32 * max(num, 1))(*[i[0] for i in inst])
+        ks = (ctypes.c_uint32 * max(num, 1))(*[len(i[1]) for i in inst])
+        offs = []
+        cols = []
+        for _, pre in inst:
+            offs.append(len(cols))
+            cols.extend(pre)
+        po = (ctypes.c_uint32 * max(num, 1))(*offs)
+        pc = (ctypes.c_uint32 * max(len(cols), 1))(*cols)
+        counts = (U128 * max(num, 1))()
+        o = options(**opts)
+        err = ctypes.create_string_buffer(512)
+        with self._lock:
+            rc = lib.qpeps_count_batch(self._h, num, ns, ks, po, pc, ctypes.byref(o), counts, err, len(err))
+        _check(rc, err)
+        return [counts[i].value for i in range(num)]
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def contract_rows(n: int, **opts) -> ContractionResult:
+    """``contract_rows(n)`` (src/lib.rs:758) on the default device."""
+    return default_context().contract_rows(n, **opts)
+
+
+def count(n: int, prefix: Sequence[int] = (), **opts) -> int:
+    return default_context().count(n, prefix, **opts)
+
+
+def known_count(n: int) -> int | None:
+    """``known_count`` (src/lib.rs:5752-5784)."""
+    out = U128()
+    rc = library().qpeps_known_count(int(n), ctypes.byref(out))
+    return None if rc != QPEPS_OK else out.value
+
+
+def certify_c(entries: Sequence[tuple[int, int]]) -> None:
+    """Run the library's CompiledRowOperator::compile check on (legs_key, value) entries."""
+    lib = library()
+    m = len(entries)
+    legs = (ctypes.c_uint32 * max(m, 1))(*[e[0] for e in entries])
+    vals = (ctypes.c_uint64 * max(m, 1))(*[e[1] for e in entries])
+    err = ctypes.create_string_buffer(512)
+    _check(lib.qpeps_certify_c(legs, vals, m, err, len(err)), err)
+
+
+def version() -> str:
+    return library().qpeps_version().decode()
+
+
+def build() -> Path:
+    from . import build as _b  # noqa: PLC0415
+
+    return _b.build()

@@ -1,0 +1,166 @@
+// Device-side building blocks of the boundary store and the key merge.
+//
+// Boundary key layout (row granularity) is the reference's PackedBoundary
+// (src/lib.rs:348-377): bits [0,n) columns, [n,2n) diag_dr, [2n,3n) diag_dl.
+// A key is held in `uint64_t` when 3n <= 63 (N <= 21) and in
+// `unsigned __int128` otherwise (N <= 42). Mid-row (site granularity) keys
+// add the row signal at bit 3n; the u64 form is used for N <= 20 there.
+//
+// Coefficients are residues modulo up to four primes just below 2^31, so the
+// sum of two residues never wraps a u32; CRT on the host rebuilds the exact
+// count.
+#pragma once
+
+#include <cstdint>
+
+namespace qpeps {
+
+using u32 = uint32_t;
+using u64 = uint64_t;
+using u128 = unsigned __int128;
+
+constexpr int kMaxResidues = 4;
+
+// The four largest primes below 2^31, in the order the CRT plan takes them.
+__host__ __device__ constexpr u32 prime_at(int r) {
+  return r == 0 ? 2147483647u : r == 1 ? 2147483629u : r == 2 ? 2147483587u : 2147483579u;
+}
+constexpr u32 kPrimes[kMaxResidues] = {prime_at(0), prime_at(1), prime_at(2), prime_at(3)};
+
+__host__ __device__ __forceinline__ u32 add_mod(u32 a, u32 b, u32 p) {
+  u32 s = a + b;  // a, b < p < 2^31: no wrap
+  return s >= p ? s - p : s;
+}
+
+__host__ __device__ __forceinline__ u32 mul_mod(u32 a, u32 b, u32 p) {
+  return (u32)(((u64)a * (u64)b) % p);
+}
+
+// splitmix64 finaliser: a bijective 64-bit mixer (Steele, Lea, Flood 2014).
+__host__ __device__ __forceinline__ u64 mix64(u64 x) {
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ULL;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebULL;
+  x ^= x >> 31;
+  return x;
+}
+
+template <typename K>
+__host__ __device__ __forceinline__ u64 key_hash(K k);
+template <>
+__host__ __device__ __forceinline__ u64 key_hash<u64>(u64 k) {
+  return mix64(k);
+}
+template <>
+__host__ __device__ __forceinline__ u64 key_hash<u128>(u128 k) {
+  return mix64((u64)k ^ mix64((u64)(k >> 64) + 0x9e3779b97f4a7c15ULL));
+}
+
+// ---- packed boundary -------------------------------------------------------
+
+struct State {
+  u64 cols, dr, dl;
+};
+
+template <typename K>
+__host__ __device__ __forceinline__ State unpack(K key, unsigned n, u64 mask) {
+  State s;
+  s.cols = (u64)key & mask;
+  s.dr = (u64)(key >> n) & mask;
+  s.dl = (u64)(key >> (2 * n)) & mask;
+  return s;
+}
+
+template <typename K>
+__host__ __device__ __forceinline__ K pack(u64 cols, u64 dr, u64 dl, unsigned n) {
+  return (K)cols | ((K)dr << n) | ((K)dl << (2 * n));
+}
+
+// Compiled row successor (src/lib.rs:600-638 after certification): place the
+// occupied C entry at free column `bit`, then move the diagonal signals to
+// their next-row positions. Signals leaving the board are contracted with v2.
+template <typename K>
+__host__ __device__ __forceinline__ K row_successor(const State& s, u64 bit, unsigned n, u64 mask) {
+  return pack<K>(s.cols | bit, ((s.dr | bit) << 1) & mask, (s.dl | bit) >> 1, n);
+}
+
+// ---- hash table slots --------------------------------------------------------
+//
+// A slot holds the bitwise complement of the key (so an all-zero slot is empty
+// and one memset clears the table; no valid key is all ones because its top
+// bit is never used) and one u64 accumulator per residue. Each contribution is
+// < 2^31 and at most 4N parents reach one key in a step, so an accumulator
+// never wraps; it is reduced modulo its prime when the table is compacted.
+
+template <typename K, int R>
+struct SlotBytes {
+  static constexpr int raw = (int)sizeof(K) + 8 * R;
+  static constexpr int value = raw <= 16 ? 16 : raw <= 32 ? 32 : 64;
+};
+
+template <typename K, int R>
+struct alignas(SlotBytes<K, R>::value) Slot {
+  K nkey;
+  u64 acc[R];
+};
+
+__device__ __forceinline__ u64 atomic_cas_key(u64* addr, u64 cmp, u64 val) {
+  return (u64)atomicCAS((unsigned long long*)addr, (unsigned long long)cmp, (unsigned long long)val);
+}
+
+// 128-bit compare-and-swap (PTX atom.cas.b128, sm_90 and later).
+__device__ __forceinline__ u128 atomic_cas_key(u128* addr, u128 cmp, u128 val) {
+  u64 cl = (u64)cmp, ch = (u64)(cmp >> 64), vl = (u64)val, vh = (u64)(val >> 64);
+  u64 ol, oh;
+  asm volatile(
+      "{\n\t.reg .b128 c, v, d;\n\t"
+      "mov.b128 c, {%2, %3};\n\t"
+      "mov.b128 v, {%4, %5};\n\t"
+      "atom.global.cas.b128 d, [%6], c, v;\n\t"
+      "mov.b128 {%0, %1}, d;\n\t}"
+      : "=l"(ol), "=l"(oh)
+      : "l"(cl), "l"(ch), "l"(vl), "l"(vh), "l"(addr)
+      : "memory");
+  return ((u128)oh << 64) | ol;
+}
+
+__device__ __forceinline__ u64 load_key_cg(const u64* p) { return __ldcg((const unsigned long long*)p); }
+__device__ __forceinline__ u128 load_key_cg(const u128* p) {
+  ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+  return ((u128)v.y << 64) | v.x;
+}
+
+// Error flags written by kernels (bit set in ErrorState::flags).
+enum ErrorBits : u32 {
+  kErrProbeLimit = 1u,  // hash probe sequence exceeded its bound (table too full)
+  kErrOverflow = 2u,    // a bounded structure overflowed its capacity
+  kErrWaitLimit = 4u,   // a bounded spin-wait gave up
+};
+
+// Insert one contribution into the global table with linear probing.
+// Returns false (and sets kErrProbeLimit) if `max_probe` slots were visited.
+template <typename K, int R>
+__device__ __forceinline__ bool table_insert(Slot<K, R>* __restrict__ table, u64 mask, K key, const u32 (&w)[R],
+                                             u32 max_probe, u32* err) {
+  const K nk = ~key;
+  u64 pos = key_hash<K>(key) & mask;
+  for (u32 probe = 0; probe < max_probe; ++probe) {
+    Slot<K, R>* s = &table[pos];
+    K cur = load_key_cg(&s->nkey);
+    if (cur == (K)0) {
+      cur = atomic_cas_key(&s->nkey, (K)0, nk);
+      if (cur == (K)0) cur = nk;
+    }
+    if (cur == nk) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) atomicAdd((unsigned long long*)&s->acc[r], (unsigned long long)w[r]);
+      return true;
+    }
+    pos = (pos + 1) & mask;
+  }
+  atomicOr(err, kErrProbeLimit);
+  return false;
+}
+
+}  // namespace qpeps

@@ -1,0 +1,74 @@
+// Internal interface between the host engine and the CUDA kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace qpeps {
+
+// Explicit local tensor C in the form the site kernel reads from constant
+// memory: for each 4-bit input signature (column_in | row_in<<1 |
+// diag_dr_in<<2 | diag_dl_in<<3, src/lib.rs:152-157) the matching entries'
+// outputs (column_out | row_out<<1 | diag_dr_out<<2 | diag_dl_out<<3) and
+// their values reduced modulo each residue prime.
+struct CTableDev {
+  uint32_t count[16];
+  uint32_t out[16][4];
+  uint32_t value_mod[16][4][4];
+};
+
+// Device view of one boundary buffer (structure of arrays).
+struct FrontierView {
+  void* keys;          // u64[cap] or u128[cap]
+  uint32_t* res;       // u32[R][cap]
+  uint64_t cap;        // entries per residue plane
+};
+
+// Per-step device scalars (one cache line each to avoid false sharing).
+struct StepScalars {
+  unsigned long long terms;          // successor terms generated
+  unsigned long long out_count;      // entries written by compaction
+  unsigned long long weight_sum[4];  // sum of residues of written entries
+  unsigned long long final_sum[4];   // sum of residues of entries with all columns set
+  unsigned long long final_states;   // entries with all columns set
+  unsigned int error;                // ErrorBits
+  unsigned int pad[7];
+};
+
+struct LaunchCfg {
+  int key_bits;  // 64 or 128
+  int residues;  // 1..4
+  int threads;   // block size of the expand kernel
+  int sms;       // SM count of the device
+};
+
+// All launchers enqueue on `stream` and return cudaGetLastError().
+cudaError_t upload_c_table(const CTableDev& table, cudaStream_t stream);
+
+// Sum over entries of popcount(free columns): the row step's successor count.
+cudaError_t launch_row_count(const LaunchCfg& cfg, const FrontierView& in, uint64_t n_in, unsigned n,
+                             StepScalars* scalars, cudaStream_t stream);
+
+// Fused compiled-row expansion + global-table insertion.
+cudaError_t launch_row_expand_insert(const LaunchCfg& cfg, const FrontierView& in, uint64_t n_in, unsigned n,
+                                     void* table, uint64_t table_slots, StepScalars* scalars, cudaStream_t stream);
+
+// Number of explicit-C terms produced at site `site` (mid-row key layout).
+cudaError_t launch_site_count(const LaunchCfg& cfg, const FrontierView& in, uint64_t n_in, unsigned n, unsigned site,
+                              StepScalars* scalars, cudaStream_t stream);
+
+// Explicit-C site update (one launch per site) + global-table insertion.
+cudaError_t launch_site_expand_insert(const LaunchCfg& cfg, const FrontierView& in, uint64_t n_in, unsigned n,
+                                      unsigned site, void* table, uint64_t table_slots, StepScalars* scalars,
+                                      cudaStream_t stream);
+
+// Table -> boundary buffer; accumulates weight sums and final (v1) sums.
+cudaError_t launch_compact(const LaunchCfg& cfg, const void* table, uint64_t table_slots, const FrontierView& out,
+                           unsigned n, bool write_out, StepScalars* scalars, cudaStream_t stream);
+
+// Bytes per table slot for a key width / residue count.
+size_t slot_bytes(int key_bits, int residues);
+
+}  // namespace qpeps

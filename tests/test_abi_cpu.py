@@ -1,0 +1,66 @@
+"""The C-ABI library loads and exports every symbol include/qpeps.h declares.
+
+CPU only: no call here launches device work. Host-only entry points
+(version, known counts, options, C certification) are exercised directly.
+"""
+from __future__ import annotations
+
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_functions():
+    text = (ROOT / "include" / "qpeps.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(qpeps_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = _declared_functions()
+    for required in ["qpeps_contract_rows", "qpeps_count", "qpeps_count_batch", "qpeps_known_count",
+                     "qpeps_ctx_create", "qpeps_ctx_destroy", "qpeps_version", "qpeps_certify_c"]:
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(qp):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(qp.LIBRARY_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT (qpeps_[a-z0-9_]+)$", out, flags=re.M))
+    missing = [n for n in _declared_functions() if n not in exported]
+    assert not missing, missing
+    lib = qp.library()
+    for n in _declared_functions():
+        getattr(lib, n)
+
+
+def test_version_and_known_counts(qp, golden):
+    assert "sm_103a" in qp.version()
+    assert [qp.known_count(n) for n in range(28)] == [int(v) for v in golden["known_count"]]
+    assert qp.known_count(28) is None
+
+
+def test_options_default_matches_reference_semantics(qp):
+    o = qp.options()
+    assert o.granularity == qp.GRAIN_ROW and o.symmetry == 1 and o.collect_layers == 1
+
+
+def test_certify_c_accepts_sec_vi_and_fails_closed(qp, oracle):
+    c = oracle.c_entries()
+    qp.certify_c(c)
+    cases = {
+        "unit Sec. VI coefficients": [(l, 2 if i == 0 else v) for i, (l, v) in enumerate(c)],
+        "missing a pass-through": c[1:],
+        "missing the occupied entry": [e for e in c if e[0] != 0b10101010],
+        "multiple occupied": c + [(0b10101010, 1)],
+        "outside the Sec. VI row automaton": c + [(0b00000010, 1)],
+        "duplicate C pass-through": c + [(0, 1)],
+    }
+    for msg, table in cases.items():
+        with pytest.raises(qp.ContractionError, match=msg) as ei:
+            qp.certify_c(table)
+        assert ei.value.code == qp.QPEPS_ERR_INVALID
+        assert oracle.compile_check(table) is not None

@@ -1,0 +1,176 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Bar: bit-exact. Counts, peak support, work counters and every per-row
+(input_states, row_operator_candidates, row_operator_matched,
+completed_row_terms, output_states, output_weight) equal the oracle's
+restatement of contract_rows (src/lib.rs:5287-5415) and the reference's
+published golden values.
+"""
+from __future__ import annotations
+
+import random
+
+import pytest
+
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+LAYER_FIELDS = ["row", "input_states", "row_operator_candidates", "row_operator_matched", "completed_row_terms",
+                "output_states", "output_weight"]
+
+
+def _gpu_layers(r):
+    return [tuple(getattr(l, f) for f in LAYER_FIELDS) for l in r.layers]
+
+
+def _oracle_layers(o):
+    return [tuple(l[f] for f in LAYER_FIELDS) for l in o["layers"]]
+
+
+@pytest.mark.parametrize("n", range(0, 13))
+def test_contract_rows_matches_oracle_row_by_row(ctx, oracle, n):
+    g = ctx.contract_rows(n)
+    o = oracle.contract(n, backend=O.SORT_REDUCE)
+    assert g.count == o["count"] == oracle.known_count(n)
+    assert g.peak_states == o["peak_states"]
+    assert g.row_operator_candidates == o["row_operator_candidates"]
+    assert g.row_operator_matched == o["row_operator_matched"]
+    assert (g.tensor_entries_examined, g.tensor_entries_matched) == (o["tensor_entries_examined"],
+                                                                    o["tensor_entries_matched"])
+    assert _gpu_layers(g) == _oracle_layers(o)
+
+
+@pytest.mark.parametrize("n", [13, 14])
+def test_orbit_path_matches_published_layers(ctx, golden, n):
+    g = ctx.contract_rows(n)
+    e12 = golden["e12_summary"]["d4_orbit_serial_sort_reduce"][str(n)]
+    assert g.count == e12["count"]
+    assert g.peak_states == e12["peak_support"]
+    assert g.row_operator_candidates == e12["row_operator_candidates"]
+    assert g.row_operator_matched == e12["row_operator_matched"]
+    assert [1] + [l.output_states for l in g.layers] == golden["orbit_layers_output_states"][str(n)]
+
+
+def test_n16_matches_published_peak_and_matched_work(ctx, golden):
+    # benchmarks/e36_joint_u64_release.csv, N=16 (orbit path)
+    g = ctx.contract_rows(16)
+    ref = golden["e36_orbit_n16"]["16"]
+    assert g.count == ref["count"] == 14772512
+    assert g.peak_states == ref["peak_support"]
+    assert g.row_operator_matched == ref["row_operator_matched"]
+    assert g.device["residues"] == 2 and g.device["key_bits"] == 64
+
+
+@pytest.mark.parametrize("n", range(1, 12))
+def test_dense_no_symmetry_matches_oracle(ctx, oracle, n):
+    g = ctx.contract_rows(n, symmetry=0)
+    o = oracle.contract(n, backend=O.SORT_REDUCE, symmetry=False)
+    assert g.count == o["count"]
+    assert g.peak_states == o["peak_states"]
+    assert _gpu_layers(g) == _oracle_layers(o)
+
+
+def test_dense_peaks_match_published(ctx, golden):
+    for n in [10, 12, 14]:
+        g = ctx.contract_rows(n, symmetry=0)
+        assert g.peak_states == golden["naive_dense_hashmap"][str(n)]["peak_support"]
+        assert g.count == golden["naive_dense_hashmap"][str(n)]["count"]
+
+
+@pytest.mark.parametrize("n", range(1, 11))
+def test_site_grain_equals_row_grain(ctx, n):
+    # One plain launch per site applying the explicit C table.
+    s = ctx.contract_rows(n, granularity=1)
+    r = ctx.contract_rows(n)
+    assert s.count == r.count
+    assert s.peak_states >= r.peak_states
+    assert [(l.input_states, l.output_states, l.output_weight, l.completed_row_terms) for l in s.layers] == [
+        (l.input_states, l.output_states, l.output_weight, l.completed_row_terms) for l in r.layers]
+
+
+@pytest.mark.parametrize("n", [1, 4, 8, 11, 12])
+def test_forced_wide_keys_are_exact(ctx, oracle, n):
+    g = ctx.contract_rows(n, key_bits=128)
+    o = oracle.contract(n)
+    assert g.device["key_bits"] == 128
+    assert g.count == o["count"]
+    assert _gpu_layers(g) == _oracle_layers(o)
+    s = ctx.contract_rows(n, key_bits=128, granularity=1)
+    assert s.count == o["count"]
+
+
+@pytest.mark.parametrize("residues", [1, 2, 3, 4])
+def test_forced_residue_planes_are_exact(ctx, oracle, residues):
+    n = 10
+    g = ctx.contract_rows(n, residues=residues)
+    assert g.device["residues"] == residues
+    assert g.count == 724
+    assert _gpu_layers(g) == _oracle_layers(oracle.contract(n))
+
+
+def test_too_few_residues_for_n_factorial_is_rejected(ctx, qp):
+    with pytest.raises(qp.ContractionError) as ei:
+        ctx.contract_rows(14, residues=1)
+    assert ei.value.code == qp.QPEPS_ERR_RANGE
+
+
+def test_rejects_virtual_boundaries_wider_than_u128_layout(ctx, qp):
+    with pytest.raises(qp.ContractionError, match="supports N <= 42") as ei:
+        ctx.contract_rows(43)
+    assert ei.value.code == qp.QPEPS_ERR_RANGE
+
+
+def test_empty_board(ctx):
+    g = ctx.contract_rows(0)
+    assert (g.count, g.peak_states, len(g.layers)) == (1, 1, 0)
+
+
+def test_prefix_counts_match_oracle(ctx, oracle):
+    rng = random.Random(20261203)
+    for _ in range(60):
+        n = rng.randint(4, 12)
+        k = rng.randint(0, 3)
+        prefix = [rng.randrange(n) for _ in range(k)]
+        want = oracle.contract(n, symmetry=False, prefix=prefix)["count"] if k else oracle.known_count(n)
+        assert ctx.count(n, prefix) == want, (n, prefix)
+
+
+def test_prefix_sum_rule_at_n14(ctx, oracle):
+    assert sum(ctx.count(14, [c]) for c in range(14)) == oracle.known_count(14)
+
+
+def test_complete_prefix_counts_itself(ctx):
+    assert ctx.count(8, [0, 4, 7, 5, 2, 6, 1, 3]) == 1
+    assert ctx.count(8, [0, 1]) == 0
+
+
+def test_count_batch_matches_individual_counts(ctx, oracle):
+    inst = [(8, []), (9, [1]), (10, [2, 5]), (6, [0, 0]), (11, [3, 0, 7])]
+    got = ctx.count_batch(inst)
+    want = [oracle.known_count(8)] + [oracle.contract(n, symmetry=False, prefix=p)["count"] for n, p in inst[1:]]
+    assert got == want
+
+
+def test_small_device_budget_splits_batches_and_stays_exact(ctx, oracle):
+    # Forced capacity pressure: batches split (and slices deepen) on the host.
+    full = ctx.contract_rows(12)
+    tight = ctx.contract_rows(12, device_budget_bytes=6 << 20)
+    assert tight.device["batches"] > 1
+    assert tight.count == full.count == oracle.known_count(12)
+
+
+def test_deeper_host_slices_are_exact(ctx, oracle):
+    for depth in [2, 3]:
+        g = ctx.contract_rows(13, slice_depth=depth)
+        assert g.count == oracle.known_count(13)
+        assert g.device["slice_depth"] == depth
+        # Merged rows after the host-seeded prefix equal the reference's frontier.
+        o = oracle.contract(13)
+        assert _gpu_layers(g) == _oracle_layers(o)
+
+
+@pytest.mark.parametrize("n", [15, 17])
+def test_full_size_counts(ctx, oracle, n):
+    g = ctx.contract_rows(n)
+    assert g.count == oracle.known_count(n)
