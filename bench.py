@@ -227,11 +227,11 @@ def run_ours(args):
 
     peak, peak_kind = measured_peaks()
     d = results[-1].device
-    merge_s = d["merge_kernel_ms"] / 1e3 if d["merge_kernel_ms"] else 0.0
     achieved = d["merge_kernel_bytes"] / max(d["device_ms"] / 1e3, 1e-12) / 1e9
     roofline = {
         "bound": "hbm",
-        "kernel": "merge step: row_expand_insert_kernel + compact_kernel (hash merge)",
+        "kernel": ("merge step: partition_scatter_kernel + partition_merge_kernel" if d["merge"] == 2
+                   else "merge step: row_expand_insert_kernel + compact_kernel (global table)"),
         "achieved": achieved,
         "peak": peak,
         "peak_kind": peak_kind,
@@ -240,8 +240,9 @@ def run_ours(args):
         "traffic": None,
         "algorithmic_bytes_per_step": d["merge_kernel_bytes"],
         "launches_per_step": d["merge_kernel_launches"],
-        "expand_insert_ms_per_step": d["merge_kernel_ms"],
-        "merge_ms_per_step": d["device_ms"],
+        "scatter_ms_per_step": d["scatter_kernel_ms"],
+        "merge_ms_per_step": d["merge_kernel_ms"],
+        "step_ms_per_step": d["device_ms"],
     }
     line = {
         "metric": METRIC,
@@ -264,6 +265,7 @@ def run_ours(args):
             "batches": d["batches"],
             "residues": d["residues"],
             "key_bits": d["key_bits"],
+            "merge": {1: "hash", 2: "partition"}.get(d["merge"], d["merge"]),
             "l2": "inputs larger than L2 (boundary buffers of GBs per row)",
             "parallelism": "replicas" if world > 1 else "single",
         },

@@ -86,7 +86,8 @@ typedef struct qpeps_result {
   uint64_t gpu_launches;      /* kernels launched by this call */
   uint64_t peak_device_bytes; /* high-water mark of the context's device pool */
   double device_ms;           /* device time of all row steps (CUDA events) */
-  double merge_kernel_ms;     /* device time of the dominant merge kernel */
+  double merge_kernel_ms;     /* device time of the merge kernel (table compact or partition merge) */
+  double scatter_kernel_ms;   /* device time of the expand kernel (table insert or partition scatter) */
   uint64_t merge_kernel_launches;
   uint64_t merge_kernel_bytes; /* algorithmic bytes of the dominant kernel */
   uint32_t residue_primes[4];

@@ -10,7 +10,7 @@ Reference (Rust crate ``nqueens-peps-naive``):
 ``contract_rows`` returns the same fields with the same meaning and raises
 ``ContractionError`` where the reference returns ``Err(String)`` (same
 message text, e.g. N > 42). The device library must be built
-(``build.py``); there is no CPU fallback: importing the module on a machine
+(``buildlib.py``); there is no CPU fallback: importing the module on a machine
 without the library or without a CUDA device raises when a context is
 needed.
 """
@@ -90,6 +90,7 @@ class Result(ctypes.Structure):
         ("peak_device_bytes", ctypes.c_uint64),
         ("device_ms", ctypes.c_double),
         ("merge_kernel_ms", ctypes.c_double),
+        ("scatter_kernel_ms", ctypes.c_double),
         ("merge_kernel_launches", ctypes.c_uint64),
         ("merge_kernel_bytes", ctypes.c_uint64),
         ("residue_primes", ctypes.c_uint32 * 4),
@@ -256,6 +257,7 @@ def _result_from(res: Result, layers: Sequence[Layer] | None) -> ContractionResu
         "peak_device_bytes": res.peak_device_bytes,
         "device_ms": res.device_ms,
         "merge_kernel_ms": res.merge_kernel_ms,
+        "scatter_kernel_ms": res.scatter_kernel_ms,
         "merge_kernel_launches": res.merge_kernel_launches,
         "merge_kernel_bytes": res.merge_kernel_bytes,
         "residue_primes": list(res.residue_primes)[: res.residues],
@@ -393,6 +395,7 @@ def version() -> str:
 
 
 def build() -> Path:
-    from . import build as _b  # noqa: PLC0415
+    """Compile libqpeps.so (sm_103a) in-tree; see buildlib.py."""
+    import importlib  # noqa: PLC0415
 
-    return _b.build()
+    return importlib.import_module(__name__ + ".buildlib").build()

@@ -1,6 +1,6 @@
 """Build the CUDA library in-tree: libqpeps.so (sm_103a) and the qpeps CLI.
 
-    python quantum-harness-peps-naive_gb300/build.py
+    python quantum-harness-peps-naive_gb300/buildlib.py
 
 Translation units are compiled in parallel with nvcc and linked into
 `libqpeps.so` next to this file (git-ignored). The CLI links against it with an
@@ -33,7 +33,7 @@ NVCC_FLAGS = ARCH + [
     "-I",
     str(INCLUDE),
 ]
-LIB_SOURCES = ["qpeps_hash_kernels.cu", "qpeps_engine.cu"]
+LIB_SOURCES = ["qpeps_hash_kernels.cu", "qpeps_partition_kernels.cu", "qpeps_engine.cu"]
 
 
 def nvcc() -> str:

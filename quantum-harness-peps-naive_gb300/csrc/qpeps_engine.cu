@@ -268,6 +268,7 @@ struct Ctx {
   std::vector<CEntryH> c;
   CTableDev c_dev;
   bool c_uploaded = false;
+  double partition_mean = 1700.0;  // target candidates per partition (slots: 2048)
 };
 
 static void buf_release(Ctx& ctx, DevBuf& b) {
@@ -370,7 +371,7 @@ struct RowAcc {
 struct RunStats {
   u64 entries_in = 0, entries_out = 0, candidates = 0, launches = 0;
   u64 peak_states = 0;
-  double device_ms = 0, merge_ms = 0;
+  double device_ms = 0, merge_ms = 0, scatter_ms = 0;
   u64 merge_launches = 0, merge_bytes = 0;
   u64 final_res[kMaxResidues] = {0, 0, 0, 0};
   unsigned batches = 0;
@@ -381,6 +382,7 @@ struct Plan {
   int R;
   int key_bits;
   int grain;
+  int merge;  // QPEPS_MERGE_HASH or QPEPS_MERGE_PARTITION
   size_t budget;
   int threads;
 };
@@ -477,6 +479,79 @@ static StepOut merge_step(Ctx& ctx, const Plan& p, int cur, u64 n_in, u64 cap_in
   return so;
 }
 
+// Row step through the partitioned merge (scatter into hash partitions, then
+// one shared-memory merge per partition).
+static StepOut merge_step_partition(Ctx& ctx, const Plan& p, int cur, u64 n_in, u64 cap_in, bool final_step,
+                                    RunStats& rs, unsigned row) {
+  LaunchCfg cfg{p.key_bits, p.R, p.threads, ctx.sms};
+  FrontierView in = view_of(p, ctx.front[cur], cap_in);
+  cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
+  cuda_check(launch_row_count(cfg, in, n_in, p.n, ctx.d_sc, ctx.stream), "row count kernel");
+  rs.launches += 1;
+  sync_scalars(ctx);
+  StepOut so{};
+  so.terms = ctx.h_sc->terms;
+  const u64 out_cap = std::max<u64>(so.terms, 1);
+  const u32 cap = partition_capacity();
+  const size_t cb = candidate_bytes(p.R);
+  double mean = ctx.partition_mean;
+  for (int attempt = 0;; ++attempt) {
+    const u64 parts64 = std::max<u64>(1, (u64)((double)so.terms / mean) + 1);
+    if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
+    const u32 parts = (u32)parts64;
+    const size_t region_bytes = (size_t)parts * cap * cb;
+    const size_t cursor_bytes = ((size_t)parts * 4 + 255) / 256 * 256;
+    const size_t out_bytes = final_step ? 0 : out_cap * entry_bytes(p);
+    const size_t need = region_bytes + cursor_bytes + out_bytes + ctx.front[cur].bytes;
+    if (need > p.budget) fail(QPEPS_ERR_CAPACITY, row_msg("device budget exceeded at row", row + 1));
+    make_room(ctx, ctx.table, region_bytes + cursor_bytes, ctx.front[1 - cur], out_bytes, p.budget);
+    buf_reserve(ctx, ctx.table, region_bytes + cursor_bytes, p.budget, "partition regions");
+    if (!final_step) buf_reserve(ctx, ctx.front[1 - cur], out_bytes, p.budget, "boundary buffer");
+    void* regions = ctx.table.ptr;
+    uint32_t* cursors = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(ctx.table.ptr) + region_bytes);
+    cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear partition cursors");
+    cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
+    FrontierView out{};
+    if (!final_step) out = view_of(p, ctx.front[1 - cur], out_cap);
+    PartitionCfg pc{p.R, ctx.sms, parts, cap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1};
+    cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+    cuda_check(launch_partition_scatter(pc, in, n_in, p.n, regions, cursors, ctx.d_sc, ctx.stream),
+               "partition scatter kernel");
+    cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+    cuda_check(launch_partition_merge(pc, regions, cursors, out, p.n, !final_step, ctx.d_sc, ctx.stream),
+               "partition merge kernel");
+    cuda_check(cudaEventRecord(ctx.ev[2], ctx.stream), "event");
+    rs.launches += 2;
+    sync_scalars(ctx);
+    if (ctx.h_sc->error & kErrOverflow) {
+      // A partition received more candidates than its slots: retry with
+      // smaller partitions (the scatter wrote nothing past a full partition).
+      if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, row_msg("partition overflow persists at row", row + 1));
+      mean *= 0.6;
+      continue;
+    }
+    if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, row_msg("device capacity error at row", row + 1));
+    float ms_scatter = 0, ms_merge = 0;
+    cudaEventElapsedTime(&ms_scatter, ctx.ev[0], ctx.ev[1]);
+    cudaEventElapsedTime(&ms_merge, ctx.ev[1], ctx.ev[2]);
+    so.out = ctx.h_sc->out_count;
+    so.out_cap = out_cap;
+    for (int r = 0; r < p.R; ++r) {
+      so.weight[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
+      so.final_sum[r] = ctx.h_sc->final_sum[r] % kPrimes[r];
+    }
+    rs.device_ms += ms_scatter + ms_merge;
+    rs.merge_ms += ms_merge;
+    rs.scatter_ms += ms_scatter;
+    rs.merge_launches += 1;
+    rs.merge_bytes += n_in * entry_bytes(p) + so.out * entry_bytes(p);
+    rs.entries_in += n_in;
+    rs.entries_out += so.out;
+    rs.candidates += so.terms;
+    return so;
+  }
+}
+
 static void upload_items(Ctx& ctx, const Plan& p, const std::vector<Item>& items, size_t lo, size_t hi, int buf,
                          u64* cap_out) {
   const u64 cnt = hi - lo;
@@ -510,6 +585,13 @@ static void run_batch(Ctx& ctx, const Plan& p, const std::vector<Item>& items, s
   std::vector<RowAcc> lrows(p.n);
   u64 cap = 0;
   int cur = 0;
+  // Every pooled buffer is dead between batches: drop them if a previous,
+  // larger call left the pool above this call's budget.
+  if (ctx.pool_bytes > p.budget / 2) {
+    buf_release(ctx, ctx.front[0]);
+    buf_release(ctx, ctx.front[1]);
+    buf_release(ctx, ctx.table);
+  }
   upload_items(ctx, p, items, lo, hi, cur, &cap);
   u64 count = hi - lo;
   local.peak_states = count;
@@ -542,7 +624,8 @@ static void run_batch(Ctx& ctx, const Plan& p, const std::vector<Item>& items, s
       }
       acc.matched = acc.completed = row_terms;
     } else {
-      so = merge_step(ctx, p, cur, count, cap, false, 0, last_row, local, row);
+      so = p.merge == QPEPS_MERGE_PARTITION ? merge_step_partition(ctx, p, cur, count, cap, last_row, local, row)
+                                            : merge_step(ctx, p, cur, count, cap, false, 0, last_row, local, row);
       count = so.out;
       if (!last_row) {
         cur = 1 - cur;
@@ -587,6 +670,7 @@ static void run_batch(Ctx& ctx, const Plan& p, const std::vector<Item>& items, s
   rs.launches += local.launches;
   rs.device_ms += local.device_ms;
   rs.merge_ms += local.merge_ms;
+  rs.scatter_ms += local.scatter_ms;
   rs.merge_launches += local.merge_launches;
   rs.merge_bytes += local.merge_bytes;
   rs.peak_states = std::max(rs.peak_states, local.peak_states);
@@ -665,6 +749,15 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o) {
     p.budget = (size_t)((double)(fr + ctx.pool_bytes) * 0.90);
   }
   p.threads = o.block_threads ? (int)o.block_threads : 256;
+  const bool partition_ok = p.key_bits == 64 && p.grain == QPEPS_GRAIN_ROW;
+  if (o.merge == QPEPS_MERGE_PARTITION && !partition_ok)
+    fail(QPEPS_ERR_INVALID, "the partitioned merge needs u64 keys and row granularity");
+  if (o.merge == QPEPS_MERGE_HASH)
+    p.merge = QPEPS_MERGE_HASH;
+  else if (o.merge == QPEPS_MERGE_PARTITION || o.merge == QPEPS_MERGE_AUTO)
+    p.merge = partition_ok ? QPEPS_MERGE_PARTITION : QPEPS_MERGE_HASH;
+  else
+    fail(QPEPS_ERR_INVALID, "unknown merge strategy");
   return p;
 }
 
@@ -850,7 +943,7 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->key_bits = n ? (uint32_t)c.plan.key_bits : 0;
   r->slice_depth = c.slice_depth;
   r->batches = c.rs.batches;
-  r->merge = QPEPS_MERGE_HASH;
+  r->merge = n ? (uint32_t)c.plan.merge : 0;
   r->entries_in = c.rs.entries_in;
   r->entries_out = c.rs.entries_out;
   r->candidates = c.rs.candidates;
@@ -858,6 +951,7 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->peak_device_bytes = ctx.peak_pool_bytes;
   r->device_ms = c.rs.device_ms;
   r->merge_kernel_ms = c.rs.merge_ms;
+  r->scatter_kernel_ms = c.rs.scatter_ms;
   r->merge_kernel_launches = c.rs.merge_launches;
   r->merge_kernel_bytes = c.rs.merge_bytes;
   for (int i = 0; i < kMaxResidues; ++i) {

@@ -71,4 +71,24 @@ cudaError_t launch_compact(const LaunchCfg& cfg, const void* table, uint64_t tab
 // Bytes per table slot for a key width / residue count.
 size_t slot_bytes(int key_bits, int residues);
 
+// Partitioned merge (u64 keys): `parts` hash partitions of `cap` candidate
+// slots each.
+struct PartitionCfg {
+  int residues;
+  int sms;
+  uint32_t parts;
+  uint32_t cap;
+  int merge_blocks_per_sm;
+};
+
+size_t candidate_bytes(int residues);
+uint32_t partition_capacity();
+
+cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
+                                     void* regions, uint32_t* cursors, StepScalars* scalars, cudaStream_t stream);
+
+cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                                   const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
+                                   cudaStream_t stream);
+
 }  // namespace qpeps

@@ -1,0 +1,427 @@
+// Partitioned key merge: one row step as two streaming kernels.
+//
+//   partition_scatter : every parent is read once (coalesced); each
+//                       (parent, free column) successor is appended to one of
+//                       P hash partitions (16-byte candidate = key + residues).
+//                       Partition tails stay in L2, so the scattered 16-byte
+//                       stores reach HBM as full sectors.
+//   partition_merge   : one CTA per partition loads its candidates (coalesced)
+//                       into a shared-memory open-addressing table, sums equal
+//                       keys' residues with shared-memory atomics, and writes
+//                       the unique entries to the next boundary buffer.
+//
+// This replaces the reference's `candidates.sort_unstable_by_key` + checked
+// reduce (src/lib.rs:5353-5367): equal packed keys are merged by addition;
+// the order of the output boundary is not observable by any metric.
+#include <cuda_runtime.h>
+
+#include "qpeps_device.cuh"
+#include "qpeps_internal.h"
+
+namespace qpeps {
+
+namespace {
+
+constexpr u32 kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ u64 pboard_mask(unsigned n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
+
+__device__ __forceinline__ int pwarp_inclusive_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int t = __shfl_up_sync(kFullMask, v, d);
+    if (lane >= d) v += t;
+  }
+  return v;
+}
+
+__device__ __forceinline__ unsigned pnth_set_bit(u64 m, int k) {
+  u32 lo = (u32)m, hi = (u32)(m >> 32);
+  int plo = __popc(lo);
+  return k < plo ? __fns(lo, 0, k + 1) : 32u + __fns(hi, 0, k - plo + 1);
+}
+
+constexpr u64 kEmptyKey = ~0ull;  // no u64 boundary key has bit 63 set (3n <= 63)
+
+// Map a 64-bit hash uniformly onto [0, parts) (multiply-high).
+__device__ __forceinline__ u32 partition_of(u64 h, u32 parts) { return (u32)(((h >> 32) * (u64)parts) >> 32); }
+
+template <int R>
+struct alignas(16) Cand {
+  u64 key;
+  u32 res[R];
+};
+
+// 16-byte vector moves of a candidate (one or two ulonglong2).
+template <int R>
+__device__ __forceinline__ void store_cand(Cand<R>* dst, const Cand<R>& c) {
+  ulonglong2* d = reinterpret_cast<ulonglong2*>(dst);
+  u64 w01 = (u64)c.res[0] | (R > 1 ? (u64)c.res[R > 1 ? 1 : 0] << 32 : 0ull);
+  d[0] = make_ulonglong2(c.key, w01);
+  if constexpr (R > 2) {
+    u64 w23 = (u64)c.res[2] | (R > 3 ? (u64)c.res[R > 3 ? 3 : 2] << 32 : 0ull);
+    d[1] = make_ulonglong2(w23, 0ull);
+  }
+}
+
+template <int R>
+__device__ __forceinline__ Cand<R> load_cand(const Cand<R>* src) {
+  const ulonglong2* s = reinterpret_cast<const ulonglong2*>(src);
+  const ulonglong2 a = __ldcs(s);
+  Cand<R> c;
+  c.key = a.x;
+  c.res[0] = (u32)a.y;
+  if constexpr (R > 1) c.res[R > 1 ? 1 : 0] = (u32)(a.y >> 32);
+  if constexpr (R > 2) {
+    const ulonglong2 b = __ldcs(s + 1);
+    c.res[R > 2 ? 2 : 0] = (u32)b.x;
+    if constexpr (R > 3) c.res[R > 3 ? 3 : 0] = (u32)(b.x >> 32);
+  }
+  return c;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ unsigned long long pblock_sum(unsigned long long v) {
+  __shared__ unsigned long long s_part[BLOCK / 32];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFullMask, v, d);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) s_part[wid] = v;
+  __syncthreads();
+  unsigned long long t = 0;
+  if (wid == 0) {
+    t = lane < BLOCK / 32 ? s_part[lane] : 0ull;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(kFullMask, t, d);
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Scatter. Each warp takes 64 parents per iteration (two per lane; the next
+// iteration's parents are loaded before this iteration's atomics are waited
+// on), flattens the ragged (parent, free column) list, and for every batch of
+// up to KB*32 successors issues all cursor atomics before any store, so each
+// lane keeps KB atomics in flight.
+
+constexpr int kPPL = 2;  // parents per lane per iteration
+constexpr int kKB = 4;   // successor rounds per atomic batch
+
+template <int R, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __restrict__ keys,
+                                                                  const u32* __restrict__ res, u64 res_stride,
+                                                                  u64 n_in, unsigned n, Cand<R>* __restrict__ regions,
+                                                                  u32* __restrict__ cursors, u32 parts, u32 cap,
+                                                                  StepScalars* __restrict__ sc) {
+  constexpr int WARPS = BLOCK / 32;
+  constexpr int PW = 32 * kPPL;  // parents per warp iteration
+  __shared__ u64 s_key[WARPS][PW];
+  __shared__ u64 s_free[WARPS][PW];
+  __shared__ u32 s_w[WARPS][R][PW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const u64 mask = pboard_mask(n);
+  const u64 gwarp = (u64)blockIdx.x * WARPS + wid;
+  const u64 stride = (u64)gridDim.x * WARPS * PW;
+  bool overflow = false;
+
+  // Prefetched parents of the next iteration (registers).
+  u64 nkey[kPPL];
+  u32 nw[kPPL][R];
+  auto fetch = [&](u64 base) {
+#pragma unroll
+    for (int q = 0; q < kPPL; ++q) {
+      const u64 i = base + q * 32 + lane;
+      nkey[q] = kEmptyKey;
+      if (i < n_in) {
+        nkey[q] = keys[i];
+#pragma unroll
+        for (int r = 0; r < R; ++r) nw[q][r] = res[r * res_stride + i];
+      }
+    }
+  };
+  u64 base = gwarp * PW;
+  if (base < n_in) fetch(base);
+  for (; base < n_in; base += stride) {
+    int cnt = 0;
+    int c0 = 0;
+#pragma unroll
+    for (int q = 0; q < kPPL; ++q) {
+      u64 fr = 0;
+      if (nkey[q] != kEmptyKey) {
+        const State s = unpack<u64>(nkey[q], n, mask);
+        fr = ~(s.cols | s.dr | s.dl) & mask;
+      }
+      s_key[wid][q * 32 + lane] = nkey[q];
+      s_free[wid][q * 32 + lane] = fr;
+#pragma unroll
+      for (int r = 0; r < R; ++r) s_w[wid][r][q * 32 + lane] = nw[q][r];
+      const int c = __popcll(fr);
+      if (q == 0) c0 = c;
+      cnt += c;
+    }
+    if (base + stride < n_in) fetch(base + stride);
+    const int incl = pwarp_inclusive_scan(cnt);
+    const int excl = incl - cnt;
+    const int total = __shfl_sync(kFullMask, incl, 31);
+    __syncwarp();
+    for (int j0 = 0; j0 < total; j0 += 32 * kKB) {
+      Cand<R> c[kKB];
+      u32 part[kKB], pos[kKB];
+#pragma unroll
+      for (int k = 0; k < kKB; ++k) {
+        const int j = j0 + k * 32 + lane;
+        int owner = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int v = __shfl_sync(kFullMask, incl, owner + step - 1);
+          if (v <= j) owner += step;
+        }
+        const int oex = __shfl_sync(kFullMask, excl, owner);
+        const int oc0 = __shfl_sync(kFullMask, c0, owner);
+        part[k] = 0xffffffffu;
+        if (j < total) {
+          int t = j - oex;
+          const int q = t < oc0 ? 0 : 1;
+          if (q) t -= oc0;
+          const int slot = q * 32 + owner;
+          const State s = unpack<u64>(s_key[wid][slot], n, mask);
+          const unsigned col = pnth_set_bit(s_free[wid][slot], t);
+          c[k].key = row_successor<u64>(s, 1ull << col, n, mask);
+#pragma unroll
+          for (int r = 0; r < R; ++r) c[k].res[r] = s_w[wid][r][slot];
+          part[k] = partition_of(mix64(c[k].key), parts);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kKB; ++k)
+        if (part[k] != 0xffffffffu) pos[k] = atomicAdd(&cursors[part[k]], 1u);
+#pragma unroll
+      for (int k = 0; k < kKB; ++k)
+        if (part[k] != 0xffffffffu) {
+          if (pos[k] < cap)
+            store_cand<R>(regions + (u64)part[k] * cap + pos[k], c[k]);
+          else
+            overflow = true;
+        }
+    }
+    __syncwarp();
+  }
+  if (overflow) atomicOr(&sc->error, kErrOverflow);
+}
+
+// ---------------------------------------------------------------------------
+// Merge. One CTA per partition at a time (persistent over partitions). All
+// candidate loads of a partition are issued together into registers; the
+// next partition's loads are issued before the current table is compacted,
+// and compaction resets the slots it reads so the table needs no separate
+// clearing pass.
+
+constexpr u64 kEmpty = kEmptyKey;
+
+template <int R, int BLOCK, int H, int CAP>
+__global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* __restrict__ regions,
+                                                                const u32* __restrict__ cursors, u32 parts,
+                                                                u64* __restrict__ keys_out, u32* __restrict__ res_out,
+                                                                u64 out_stride, unsigned n, int write_out,
+                                                                StepScalars* __restrict__ sc) {
+  constexpr int WARPS = BLOCK / 32;
+  constexpr int PER = H / BLOCK;    // table slots per thread
+  constexpr int LPT = CAP / BLOCK;  // candidate loads per thread
+  static_assert(H % BLOCK == 0 && CAP % BLOCK == 0 && PER <= 32 && (PER * WARPS) % 32 == 0, "shape");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u64* s_key = reinterpret_cast<u64*>(smem_raw);
+  unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [R][H]
+  __shared__ u32 s_cnt[PER * WARPS];
+  __shared__ unsigned long long s_base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const u64 mask = pboard_mask(n);
+  unsigned long long wsum[R], fsum[R], fstates = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
+
+  for (int i = threadIdx.x; i < H; i += BLOCK) {
+    s_key[i] = kEmpty;
+#pragma unroll
+    for (int r = 0; r < R; ++r) s_acc[r * H + i] = 0ull;
+  }
+
+  Cand<R> buf[LPT];
+  u32 bcnt = 0;
+  auto fetch = [&](u32 part) {
+    bcnt = min(cursors[part], (u32)CAP);
+    const Cand<R>* src = regions + (u64)part * CAP;
+#pragma unroll
+    for (int l = 0; l < LPT; ++l) {
+      const u32 i = l * BLOCK + threadIdx.x;
+      if (i < bcnt) buf[l] = load_cand<R>(src + i);
+    }
+  };
+  u32 part = blockIdx.x;
+  if (part < parts) fetch(part);
+  __syncthreads();
+  for (; part < parts; part += gridDim.x) {
+    // Insert the fetched candidates.
+#pragma unroll
+    for (int l = 0; l < LPT; ++l) {
+      const u32 i = l * BLOCK + threadIdx.x;
+      if (i < bcnt) {
+        const Cand<R>& c = buf[l];
+        u32 slot = (u32)mix64(c.key) & (H - 1);
+        for (int probe = 0; probe < H; ++probe) {
+          u64 cur = s_key[slot];
+          if (cur == kEmpty) {
+            cur = atomicCAS(reinterpret_cast<unsigned long long*>(&s_key[slot]), kEmpty, c.key);
+            if (cur == kEmpty) cur = c.key;
+          }
+          if (cur == c.key) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slot], (unsigned long long)c.res[r]);
+            break;
+          }
+          slot = (slot + 1) & (H - 1);
+        }
+      }
+    }
+    __syncthreads();
+    // Prefetch the next partition while this one is compacted.
+    const u32 next = part + gridDim.x;
+    if (next < parts) fetch(next);
+    // Compaction: slot it*BLOCK + tid belongs to this thread (conflict-free,
+    // coalesced); one warp scans the PER x WARPS ballot counts.
+    u32 flags = 0;
+#pragma unroll
+    for (int it = 0; it < PER; ++it) {
+      const bool occ = s_key[it * BLOCK + threadIdx.x] != kEmpty;
+      flags |= (u32)occ << it;
+      const u32 b = __ballot_sync(kFullMask, occ);
+      if (lane == 0) s_cnt[it * WARPS + wid] = __popc(b);
+    }
+    __syncthreads();
+    if (wid == 0) {
+      constexpr int PL = PER * WARPS / 32;  // counts per lane
+      u32 v[PL];
+      u32 sum = 0;
+#pragma unroll
+      for (int q = 0; q < PL; ++q) {
+        v[q] = s_cnt[lane * PL + q];
+        sum += v[q];
+      }
+      const int incl = pwarp_inclusive_scan((int)sum);
+      u32 run = (u32)incl - sum;
+#pragma unroll
+      for (int q = 0; q < PL; ++q) {
+        s_cnt[lane * PL + q] = run;
+        run += v[q];
+      }
+      const int tot = __shfl_sync(kFullMask, incl, 31);
+      if (lane == 0) s_base = tot ? atomicAdd(&sc->out_count, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    const unsigned long long base = s_base;
+#pragma unroll
+    for (int it = 0; it < PER; ++it) {
+      const bool occ = (flags >> it) & 1u;
+      const u32 b = __ballot_sync(kFullMask, occ);
+      if (occ) {
+        const int slot = it * BLOCK + threadIdx.x;
+        const u64 key = s_key[slot];
+        const u64 idx = base + s_cnt[it * WARPS + wid] + __popc(b & ((1u << lane) - 1u));
+        const bool full = (key & mask) == mask;
+        if (write_out) keys_out[idx] = key;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const u32 v = (u32)(s_acc[r * H + slot] % prime_at(r));
+          if (write_out) res_out[r * out_stride + idx] = v;
+          wsum[r] += v;
+          if (full) fsum[r] += v;
+          s_acc[r * H + slot] = 0ull;
+        }
+        s_key[slot] = kEmpty;
+        fstates += full;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    unsigned long long t = pblock_sum<BLOCK>(wsum[r]);
+    if (threadIdx.x == 0 && t) atomicAdd(&sc->weight_sum[r], t);
+    t = pblock_sum<BLOCK>(fsum[r]);
+    if (threadIdx.x == 0 && t) atomicAdd(&sc->final_sum[r], t);
+  }
+  const unsigned long long t = pblock_sum<BLOCK>(fstates);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+}
+
+constexpr int kScatterBlock = 256;
+constexpr int kMergeBlock = 512;
+constexpr int kMergeH = 4096;
+constexpr int kMergeCap = kMergeH / 2;
+
+template <int R>
+constexpr size_t merge_smem() {
+  return (size_t)kMergeH * (8 + 8 * R);
+}
+
+template <int R>
+cudaError_t scatter_impl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, unsigned n, void* regions,
+                         u32* cursors, StepScalars* sc, cudaStream_t stream) {
+  u64 want = (n_in + kScatterBlock * kPPL - 1) / (kScatterBlock * kPPL);
+  const u64 capb = (u64)pc.sms * 8;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
+  partition_scatter_kernel<R, kScatterBlock><<<grid, kScatterBlock, 0, stream>>>(
+      reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, n, reinterpret_cast<Cand<R>*>(regions), cursors,
+      pc.parts, pc.cap, sc);
+  return cudaGetLastError();
+}
+
+template <int R>
+cudaError_t merge_impl(const PartitionCfg& pc, const void* regions, const u32* cursors, const FrontierView& out,
+                       unsigned n, bool write_out, StepScalars* sc, cudaStream_t stream) {
+  auto kern = partition_merge_kernel<R, kMergeBlock, kMergeH, kMergeCap>;
+  const size_t smem = merge_smem<R>();
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const u64 capb = (u64)pc.sms * pc.merge_blocks_per_sm;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, capb));
+  kern<<<grid, kMergeBlock, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors, pc.parts,
+                                            reinterpret_cast<u64*>(out.keys), out.res, out.cap, n, write_out ? 1 : 0,
+                                            sc);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t candidate_bytes(int residues) { return residues <= 2 ? 16 : 32; }
+uint32_t partition_capacity() { return kMergeCap; }
+
+cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
+                                     void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
+  if (n_in == 0) return cudaSuccess;
+  switch (pc.residues) {
+    case 1: return scatter_impl<1>(pc, in, n_in, n, regions, cursors, sc, stream);
+    case 2: return scatter_impl<2>(pc, in, n_in, n, regions, cursors, sc, stream);
+    case 3: return scatter_impl<3>(pc, in, n_in, n, regions, cursors, sc, stream);
+    case 4: return scatter_impl<4>(pc, in, n_in, n, regions, cursors, sc, stream);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                                   const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
+                                   cudaStream_t stream) {
+  switch (pc.residues) {
+    case 1: return merge_impl<1>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 2: return merge_impl<2>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 3: return merge_impl<3>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 4: return merge_impl<4>(pc, regions, cursors, out, n, write_out, sc, stream);
+  }
+  return cudaErrorInvalidValue;
+}
+
+static_assert(sizeof(Cand<1>) == 16 && sizeof(Cand<2>) == 16 && sizeof(Cand<3>) == 32 && sizeof(Cand<4>) == 32,
+              "candidate sizes must match candidate_bytes()");
+
+}  // namespace qpeps

@@ -152,10 +152,12 @@ def test_count_batch_matches_individual_counts(ctx, oracle):
     assert got == want
 
 
-def test_small_device_budget_splits_batches_and_stays_exact(ctx, oracle):
+@pytest.mark.parametrize("merge", [1, 2])
+def test_small_device_budget_splits_batches_and_stays_exact(ctx, oracle, merge):
     # Forced capacity pressure: batches split (and slices deepen) on the host.
-    full = ctx.contract_rows(12)
-    tight = ctx.contract_rows(12, device_budget_bytes=6 << 20)
+    full = ctx.contract_rows(12, merge=merge)
+    tight = ctx.contract_rows(12, merge=merge, device_budget_bytes=1536 << 10)
+    assert full.device["batches"] == 1
     assert tight.device["batches"] > 1
     assert tight.count == full.count == oracle.known_count(12)
 
@@ -174,3 +176,30 @@ def test_deeper_host_slices_are_exact(ctx, oracle):
 def test_full_size_counts(ctx, oracle, n):
     g = ctx.contract_rows(n)
     assert g.count == oracle.known_count(n)
+
+
+@pytest.mark.parametrize("merge", [1, 2])
+@pytest.mark.parametrize("n", [5, 8, 11, 12, 13])
+def test_both_merge_strategies_match_oracle(ctx, oracle, qp, n, merge):
+    g = ctx.contract_rows(n, merge=merge)
+    assert g.device["merge"] == merge
+    o = oracle.contract(n)
+    assert g.count == o["count"]
+    assert g.peak_states == o["peak_states"]
+    assert _gpu_layers(g) == _oracle_layers(o)
+
+
+def test_partition_merge_is_default_for_u64_keys(ctx, qp):
+    assert ctx.contract_rows(12).device["merge"] == qp.MERGE_PARTITION
+    assert ctx.contract_rows(12, key_bits=128).device["merge"] == qp.MERGE_HASH
+    assert ctx.contract_rows(9, granularity=1).device["merge"] == qp.MERGE_HASH
+    with pytest.raises(qp.ContractionError):
+        ctx.contract_rows(9, granularity=1, merge=qp.MERGE_PARTITION)
+
+
+def test_n16_hash_and_partition_agree(ctx, golden):
+    a = ctx.contract_rows(16, merge=1)
+    b = ctx.contract_rows(16, merge=2)
+    assert a.count == b.count == 14772512
+    assert [(l.output_states, l.output_weight) for l in a.layers] == [(l.output_states, l.output_weight) for l in b.layers]
+    assert b.peak_states == golden["e36_orbit_n16"]["16"]["peak_support"]
