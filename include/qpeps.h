@@ -162,6 +162,30 @@ int qpeps_count_batch(void* ctx, uint32_t num, const uint32_t* n, const uint32_t
  * own C. */
 int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len);
 
+/* One row step of the partitioned merge that allocates no device memory.
+ * No counterpart in the reference (its Rust driver owns all memory).
+ *
+ * For callers that cannot call cudaMalloc, e.g. a host framework whose
+ * caching allocator owns the GPU's memory, or a serving loop that must not
+ * let an allocation synchronise the device. The caller passes device
+ * pointers: the boundary `keys_in[n_in]` (packed u64 keys, N <= 21) with
+ * residue planes `res_in[r * n_in + i]`, and output buffers
+ * `keys_out[out_cap]`, `res_out[r * out_cap + i]`; `out_cap` must be at
+ * least the step's successor count (n * n_in always suffices). Scratch comes
+ * from a fixed 48 MiB device array inside the library (held by every GPU that
+ * loads it until exit); a step whose successors do not fit is rejected with
+ * QPEPS_ERR_CAPACITY. The first call on a device looks up that array's
+ * address, so make it before any stream capture. Calls share the array:
+ * calls whose GPU work overlaps race and must be serialised by the caller.
+ * Synchronous on `stream` (NULL = default stream). Outputs: `*out_count`
+ * entries written, and per residue r the sums (mod prime r) of all written
+ * residues (`weight_residues`) and of those whose columns are all set
+ * (`final_residues`, the count after the last row); either may be NULL. */
+int qpeps_row_step_noalloc(uint32_t n, uint32_t residues, const uint64_t* keys_in, const uint32_t* res_in,
+                           uint64_t n_in, uint64_t* keys_out, uint32_t* res_out, uint64_t out_cap, void* stream,
+                           uint64_t* out_count, uint64_t* weight_residues, uint64_t* final_residues, char* err,
+                           size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -138,6 +138,12 @@ _SIGNATURES = {
          ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(Options),
          ctypes.POINTER(U128), ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "qpeps_row_step_noalloc": (
+        ctypes.c_int,
+        [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+         ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "qpeps_certify_c": (
         ctypes.c_int,
         [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_char_p,
