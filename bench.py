@@ -184,6 +184,8 @@ def run_ours(args):
         opts["slice_depth"] = args.slice_depth
     if args.grain == "site":
         opts["granularity"] = pkg.GRAIN_SITE
+    if args.tail_row is not None:
+        opts["tail_row"] = args.tail_row
 
     def barrier():
         if world > 1:
@@ -301,6 +303,8 @@ def main():
     ap.add_argument("--n", type=int, default=18)
     ap.add_argument("--grain", choices=["row", "site"], default="row")
     ap.add_argument("--slice-depth", type=int, default=0)
+    ap.add_argument("--tail-row", type=int, default=None,
+                    help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -90,6 +90,11 @@ typedef struct qpeps_result {
   double scatter_kernel_ms;   /* device time of the expand kernel (table insert or partition scatter) */
   uint64_t merge_kernel_launches;
   uint64_t merge_kernel_bytes; /* algorithmic bytes of the dominant kernel */
+  uint32_t tail_row;          /* first row contracted by the slice-tail kernel (N = none) */
+  uint32_t pad0;
+  uint64_t tail_items;        /* boundary entries handed to the slice-tail kernel */
+  uint64_t tail_overflow;     /* of those, entries redone by the row engine */
+  double tail_kernel_ms;      /* device time of the slice-tail kernel */
   uint32_t residue_primes[4];
   uint64_t count_residues[4];
 } qpeps_result;
@@ -113,6 +118,10 @@ typedef struct qpeps_options {
   uint32_t block_threads;        /* 0 = auto */
   uint32_t use_graph;            /* 1 = replay row steps through captured CUDA graphs */
   uint64_t device_budget_bytes;  /* 0 = auto (a fraction of free device memory) */
+  uint32_t tail_row;             /* rows >= tail_row run in the slice-tail kernel (a CTA contracts
+                                    batches of boundary entries in shared memory); 0 = auto (never),
+                                    >= N = never */
+  uint32_t reserved;
 } qpeps_options;
 
 /* Library version string, e.g. "qpeps-gb300 0.1.0 (sm_103a)". */

@@ -90,6 +90,9 @@ def lib() -> ctypes.CDLL:
                 P(OqU128), ctypes.c_uint64, P(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t,
             ]
             L.oracle_known_count.argtypes = [ctypes.c_uint32, P(OqU128)]
+            L.oracle_contract_from.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P(OqU128), P(OqU128),
+                                               ctypes.c_uint64, P(OqResult), P(OqLayer), ctypes.c_uint32,
+                                               ctypes.c_char_p, ctypes.c_size_t]
             L.oracle_dfs_count.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P(OqU128), ctypes.c_char_p, ctypes.c_size_t]
             L.oracle_brute_force_count.argtypes = [ctypes.c_uint32, P(OqU128)]
             L.oracle_crt_plan.argtypes = [ctypes.c_uint32, P(ctypes.c_uint64), P(ctypes.c_uint32), P(OqU128),
@@ -161,6 +164,26 @@ def contract(n: int, backend: int = SORT_REDUCE, symmetry: bool = True, sparse: 
             raise OracleError(err.value.decode())
         out["boundary"] = [(keys[i].value, weights[i].value) for i in range(m)]
     return out
+
+
+def contract_from(n: int, row0: int, boundary) -> dict:
+    """Contract rows [row0, n) from a list of (packed key, weight) pairs."""
+    L = lib()
+    m = len(boundary)
+    keys = (OqU128 * max(m, 1))(*[_u128(k) for k, _ in boundary])
+    ws = (OqU128 * max(m, 1))(*[_u128(w) for _, w in boundary])
+    res = OqResult()
+    cap = n + 1
+    layers = (OqLayer * cap)()
+    err = ctypes.create_string_buffer(512)
+    if L.oracle_contract_from(n, row0, keys, ws, m, ctypes.byref(res), layers, cap, err, len(err)):
+        raise OracleError(err.value.decode())
+    return {
+        "count": res.count.value,
+        "peak_states": res.peak_states,
+        "layers": [{"input_states": layers[i].input_states, "output_states": layers[i].output_states,
+                    "completed_row_terms": layers[i].completed_row_terms.value} for i in range(res.n_layers)],
+    }
 
 
 def known_count(n: int):

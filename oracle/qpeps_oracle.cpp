@@ -1075,6 +1075,34 @@ int oracle_contract(uint32_t n, int backend, int symmetry, int position, uint32_
   }
 }
 
+// Contract rows [row0, n) from an arbitrary boundary (packed keys + weights),
+// with the serial sort-reduce driver and no orbit weighting. Used to check
+// slice and batch decompositions: the count of a boundary is linear in it.
+int oracle_contract_from(uint32_t n, uint32_t row0, const oq_u128* keys, const oq_u128* weights, uint64_t len,
+                         oq_result* out, oq_layer* layers, uint32_t layers_cap, char* err, size_t err_len) {
+  try {
+    if (n > 42) throw Error{"the packed u128 virtual-boundary backend supports N <= 42"};
+    DriverOptions opt;
+    opt.rows = n;
+    opt.row0 = row0;
+    for (uint64_t i = 0; i < len; ++i) opt.initial.push_back(KV{from_oq(keys[i]), from_oq(weights[i])});
+    if (opt.initial.empty()) {
+      ContractionResult r{};
+      r.n = n;
+      export_result(r, out, layers, layers_cap);
+      return 0;
+    }
+    std::sort(opt.initial.begin(), opt.initial.end(), [](const KV& a, const KV& b) { return a.first < b.first; });
+    reduce_sorted(opt.initial, row0);
+    ContractionResult r = contract_rows_sort_reduce_with_modes(n, Symmetry::None, Position::Dense, opt);
+    export_result(r, out, layers, layers_cap);
+    return 0;
+  } catch (const Error& e) {
+    set_err(err, err_len, e.msg);
+    return 1;
+  }
+}
+
 int oracle_known_count(uint32_t n, oq_u128* out) {
   u128 v;
   if (!known_count(n, &v)) return 1;

@@ -93,6 +93,11 @@ class Result(ctypes.Structure):
         ("scatter_kernel_ms", ctypes.c_double),
         ("merge_kernel_launches", ctypes.c_uint64),
         ("merge_kernel_bytes", ctypes.c_uint64),
+        ("tail_row", ctypes.c_uint32),
+        ("pad0", ctypes.c_uint32),
+        ("tail_items", ctypes.c_uint64),
+        ("tail_overflow", ctypes.c_uint64),
+        ("tail_kernel_ms", ctypes.c_double),
         ("residue_primes", ctypes.c_uint32 * 4),
         ("count_residues", ctypes.c_uint64 * 4),
     ]
@@ -111,6 +116,8 @@ class Options(ctypes.Structure):
         ("block_threads", ctypes.c_uint32),
         ("use_graph", ctypes.c_uint32),
         ("device_budget_bytes", ctypes.c_uint64),
+        ("tail_row", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
 
@@ -266,6 +273,10 @@ def _result_from(res: Result, layers: Sequence[Layer] | None) -> ContractionResu
         "scatter_kernel_ms": res.scatter_kernel_ms,
         "merge_kernel_launches": res.merge_kernel_launches,
         "merge_kernel_bytes": res.merge_kernel_bytes,
+        "tail_row": res.tail_row,
+        "tail_items": res.tail_items,
+        "tail_overflow": res.tail_overflow,
+        "tail_kernel_ms": res.tail_kernel_ms,
         "residue_primes": list(res.residue_primes)[: res.residues],
         "count_residues": list(res.count_residues)[: res.residues],
     }

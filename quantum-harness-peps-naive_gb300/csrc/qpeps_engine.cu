@@ -268,7 +268,8 @@ struct Ctx {
   std::vector<CEntryH> c;
   CTableDev c_dev;
   bool c_uploaded = false;
-  double partition_mean = 1700.0;  // target candidates per partition (slots: 2048)
+  double partition_fill = 0.83;  // target candidates per partition / partition slots
+  DevBuf tail;                   // TailControl + overflow list
 };
 
 static void buf_release(Ctx& ctx, DevBuf& b) {
@@ -297,25 +298,13 @@ static void buf_reserve(Ctx& ctx, DevBuf& b, size_t bytes, size_t budget, const 
   ctx.peak_pool_bytes = std::max(ctx.peak_pool_bytes, ctx.pool_bytes);
 }
 
-// Buffers whose contents are dead at this point (the table and the output
-// boundary buffer) are released when too small, or when their oversize from an
-// earlier, larger row would push the pool past the budget.
-static void make_room(Ctx& ctx, DevBuf& a, size_t a_bytes, DevBuf& b, size_t b_bytes, size_t budget) {
-  if (a.bytes < a_bytes) buf_release(ctx, a);
-  if (b.bytes < b_bytes) buf_release(ctx, b);
-  const size_t pending = (a.ptr ? 0 : a_bytes) + (b.ptr ? 0 : b_bytes);
-  if (ctx.pool_bytes + pending > budget) {
-    buf_release(ctx, a);
-    buf_release(ctx, b);
-  }
-}
-
 static void ctx_free(Ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   buf_release(*ctx, ctx->front[0]);
   buf_release(*ctx, ctx->front[1]);
   buf_release(*ctx, ctx->table);
+  buf_release(*ctx, ctx->tail);
   if (ctx->d_sc) cudaFree(ctx->d_sc);
   if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
   for (auto& e : ctx->ev)
@@ -371,7 +360,8 @@ struct RowAcc {
 struct RunStats {
   u64 entries_in = 0, entries_out = 0, candidates = 0, launches = 0;
   u64 peak_states = 0;
-  double device_ms = 0, merge_ms = 0, scatter_ms = 0;
+  u64 tail_items = 0, tail_overflow = 0;
+  double device_ms = 0, merge_ms = 0, scatter_ms = 0, tail_ms = 0;
   u64 merge_launches = 0, merge_bytes = 0;
   u64 final_res[kMaxResidues] = {0, 0, 0, 0};
   unsigned batches = 0;
@@ -385,6 +375,7 @@ struct Plan {
   int merge;  // QPEPS_MERGE_HASH or QPEPS_MERGE_PARTITION
   size_t budget;
   int threads;
+  unsigned tail_row;  // rows >= tail_row go to the slice-tail kernel (n = none)
 };
 
 static size_t entry_bytes(const Plan& p) { return (size_t)(p.key_bits / 8) + 4u * p.R; }
@@ -409,272 +400,405 @@ static void sync_scalars(Ctx& ctx) {
   cuda_check(cudaStreamSynchronize(ctx.stream), "step synchronize");
 }
 
-// One merge step (a full row in row grain, one site in site grain).
-// Input entries are in front[cur] with capacity `cap_in`; output goes to
-// front[1-cur]. Returns the number of output entries.
-struct StepOut {
-  u64 terms, out;
-  u64 weight[kMaxResidues];
-  u64 final_sum[kMaxResidues];
-  u64 out_cap;
+// The live device boundary: ctx.front[0] holds `count` entries, keys first,
+// then R residue planes of stride `cap`. Merge steps run in place: the expand
+// kernel consumes every input entry before the merge kernel writes outputs
+// into the same buffer.
+struct DevFrontier {
+  u64 count = 0;
+  u64 cap = 0;
 };
 
-static StepOut merge_step(Ctx& ctx, const Plan& p, int cur, u64 n_in, u64 cap_in, bool site, unsigned site_idx,
-                          bool final_step, RunStats& rs, unsigned row) {
-  LaunchCfg cfg{p.key_bits, p.R, p.threads, ctx.sms};
-  FrontierView in = view_of(p, ctx.front[cur], cap_in);
-  cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-  if (site)
-    cuda_check(launch_site_count(cfg, in, n_in, p.n, site_idx, ctx.d_sc, ctx.stream), "site count kernel");
-  else
-    cuda_check(launch_row_count(cfg, in, n_in, p.n, ctx.d_sc, ctx.stream), "row count kernel");
-  rs.launches += 1;
-  sync_scalars(ctx);
-  StepOut so{};
-  so.terms = ctx.h_sc->terms;
-  const u64 slots = pow2_at_least(std::max<u64>(1024, so.terms * 2));
-  const size_t sb = slot_bytes(p.key_bits, p.R);
-  const u64 out_cap = std::max<u64>(so.terms, 1);
-  // Capacity plan for this step: table + output buffer (input already held).
-  const size_t table_bytes = slots * sb;
-  const size_t out_bytes = final_step ? 0 : out_cap * entry_bytes(p);
-  const size_t need = table_bytes + out_bytes + ctx.front[cur].bytes;
-  if (need > p.budget) fail(QPEPS_ERR_CAPACITY, row_msg("device budget exceeded at row", row + 1));
-  make_room(ctx, ctx.table, table_bytes, ctx.front[1 - cur], out_bytes, p.budget);
-  buf_reserve(ctx, ctx.table, table_bytes, p.budget, "hash table");
-  if (!final_step) buf_reserve(ctx, ctx.front[1 - cur], out_bytes, p.budget, "boundary buffer");
-  cuda_check(cudaMemsetAsync(ctx.table.ptr, 0, slots * sb, ctx.stream), "clear hash table");
-  FrontierView out{};
-  if (!final_step) out = view_of(p, ctx.front[1 - cur], out_cap);
-  cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
-  if (site)
-    cuda_check(launch_site_expand_insert(cfg, in, n_in, p.n, site_idx, ctx.table.ptr, slots, ctx.d_sc, ctx.stream),
-               "site expand-insert kernel");
-  else
-    cuda_check(launch_row_expand_insert(cfg, in, n_in, p.n, ctx.table.ptr, slots, ctx.d_sc, ctx.stream),
-               "row expand-insert kernel");
-  cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
-  cuda_check(launch_compact(cfg, ctx.table.ptr, slots, out, p.n, !final_step, ctx.d_sc, ctx.stream), "compact kernel");
-  cuda_check(cudaEventRecord(ctx.ev[2], ctx.stream), "event");
-  rs.launches += 2;
-  sync_scalars(ctx);
-  if (ctx.h_sc->error & kErrProbeLimit) fail(QPEPS_ERR_CAPACITY, row_msg("hash probe bound exceeded at row", row + 1));
-  if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, row_msg("device capacity error at row", row + 1));
-  float ms_insert = 0, ms_compact = 0;
-  cudaEventElapsedTime(&ms_insert, ctx.ev[0], ctx.ev[1]);
-  cudaEventElapsedTime(&ms_compact, ctx.ev[1], ctx.ev[2]);
-  so.out = ctx.h_sc->out_count;
-  so.out_cap = out_cap;
-  for (int r = 0; r < p.R; ++r) {
-    so.weight[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
-    so.final_sum[r] = ctx.h_sc->final_sum[r] % kPrimes[r];
+// Boundary entries parked on the host (the seed, or a half split off under
+// memory pressure), resuming at (row, site).
+struct HostChunk {
+  unsigned row = 0, site = 0;
+  bool row_counted = false;  // site grain: this row's metrics already include these entries
+  bool no_tail = false;      // entries that overflowed the slice tail: contract every row here
+  u64 count = 0;
+  std::vector<uint8_t> keys;
+  std::vector<uint32_t> res;  // R planes of `count`
+};
+
+struct StepOut {
+  u64 in = 0, terms = 0, out = 0;
+  u64 weight[kMaxResidues] = {0, 0, 0, 0};
+  u64 final_sum[kMaxResidues] = {0, 0, 0, 0};
+};
+
+enum class StepStatus { Ok, NeedSplit };
+
+static size_t key_bytes(const Plan& p) { return (size_t)p.key_bits / 8; }
+
+// Grow front[0] to hold `need` entries, keeping the live ones. Returns false
+// when the budget cannot hold the grown buffer next to `other_bytes`.
+static bool ensure_front(Ctx& ctx, const Plan& p, DevFrontier& f, u64 need, size_t other_bytes) {
+  if (f.cap >= need) return true;
+  const size_t eb = entry_bytes(p);
+  // Grow in large steps (x3, capped where the step's scratch would no longer
+  // fit next to the boundary) so that a growing frontier is copied rarely.
+  const u64 step_cap = (u64)((double)p.budget / ((double)eb + 1.25 * (double)candidate_bytes(p.R)));
+  u64 want = std::max<u64>(need, std::min<u64>(need * 3, step_cap));
+  const size_t live = ctx.front[0].bytes;
+  if (live + want * eb + other_bytes > p.budget) want = need;
+  if (live + want * eb + other_bytes > p.budget) return false;
+  DevBuf nb;
+  cudaError_t e = cudaMalloc(&nb.ptr, want * eb);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
   }
-  rs.device_ms += ms_insert + ms_compact;
-  rs.merge_ms += ms_insert;
-  rs.merge_launches += 1;
-  rs.merge_bytes += n_in * entry_bytes(p) + so.out * entry_bytes(p);
-  rs.entries_in += n_in;
-  rs.entries_out += so.out;
-  rs.candidates += so.terms;
-  return so;
+  nb.bytes = want * eb;
+  ctx.pool_bytes += nb.bytes;
+  ctx.peak_pool_bytes = std::max(ctx.peak_pool_bytes, ctx.pool_bytes);
+  if (f.count) {
+    const size_t kb = key_bytes(p);
+    char* src = static_cast<char*>(ctx.front[0].ptr);
+    char* dst = static_cast<char*>(nb.ptr);
+    cuda_check(cudaMemcpyAsync(dst, src, f.count * kb, cudaMemcpyDeviceToDevice, ctx.stream), "grow keys");
+    for (int r = 0; r < p.R; ++r)
+      cuda_check(cudaMemcpyAsync(dst + want * kb + (size_t)r * want * 4, src + f.cap * kb + (size_t)r * f.cap * 4,
+                                 f.count * 4, cudaMemcpyDeviceToDevice, ctx.stream),
+                 "grow residues");
+    cuda_check(cudaStreamSynchronize(ctx.stream), "grow synchronize");
+  }
+  buf_release(ctx, ctx.front[0]);
+  ctx.front[0] = nb;
+  f.cap = want;
+  return true;
 }
 
-// Row step through the partitioned merge (scatter into hash partitions, then
-// one shared-memory merge per partition).
-static StepOut merge_step_partition(Ctx& ctx, const Plan& p, int cur, u64 n_in, u64 cap_in, bool final_step,
-                                    RunStats& rs, unsigned row) {
+static u64 count_terms(Ctx& ctx, const Plan& p, const DevFrontier& f, bool site, unsigned site_idx, RunStats& rs) {
+  if (f.count == 0) return 0;
   LaunchCfg cfg{p.key_bits, p.R, p.threads, ctx.sms};
-  FrontierView in = view_of(p, ctx.front[cur], cap_in);
+  FrontierView in = view_of(p, ctx.front[0], f.cap);
   cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-  cuda_check(launch_row_count(cfg, in, n_in, p.n, ctx.d_sc, ctx.stream), "row count kernel");
+  if (site)
+    cuda_check(launch_site_count(cfg, in, f.count, p.n, site_idx, ctx.d_sc, ctx.stream), "site count kernel");
+  else
+    cuda_check(launch_row_count(cfg, in, f.count, p.n, ctx.d_sc, ctx.stream), "row count kernel");
   rs.launches += 1;
   sync_scalars(ctx);
-  StepOut so{};
-  so.terms = ctx.h_sc->terms;
-  const u64 out_cap = std::max<u64>(so.terms, 1);
-  const u32 cap = partition_capacity();
-  const size_t cb = candidate_bytes(p.R);
-  double mean = ctx.partition_mean;
+  return ctx.h_sc->terms;
+}
+
+// One merge step (a row in row grain, a site in site grain), in place.
+static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site, unsigned site_idx, bool final_step,
+                             RunStats& rs, unsigned row, StepOut* so_out) {
+  StepOut so;
+  const u64 n_in = f.count;
+  so.in = n_in;
+  so.terms = count_terms(ctx, p, f, site, site_idx, rs);
+  if (so.terms == 0) {
+    f.count = 0;
+    *so_out = so;
+    return StepStatus::Ok;
+  }
+  const bool partition = p.merge == QPEPS_MERGE_PARTITION && !site;
+  const size_t eb = entry_bytes(p);
+  const u32 pcap = cluster_partition_capacity();
+  double mean = ctx.partition_fill * pcap;
   for (int attempt = 0;; ++attempt) {
-    const u64 parts64 = std::max<u64>(1, (u64)((double)so.terms / mean) + 1);
-    if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
-    const u32 parts = (u32)parts64;
-    const size_t region_bytes = (size_t)parts * cap * cb;
-    const size_t cursor_bytes = ((size_t)parts * 4 + 255) / 256 * 256;
-    const size_t out_bytes = final_step ? 0 : out_cap * entry_bytes(p);
-    const size_t need = region_bytes + cursor_bytes + out_bytes + ctx.front[cur].bytes;
-    if (need > p.budget) fail(QPEPS_ERR_CAPACITY, row_msg("device budget exceeded at row", row + 1));
-    make_room(ctx, ctx.table, region_bytes + cursor_bytes, ctx.front[1 - cur], out_bytes, p.budget);
-    buf_reserve(ctx, ctx.table, region_bytes + cursor_bytes, p.budget, "partition regions");
-    if (!final_step) buf_reserve(ctx, ctx.front[1 - cur], out_bytes, p.budget, "boundary buffer");
-    void* regions = ctx.table.ptr;
-    uint32_t* cursors = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(ctx.table.ptr) + region_bytes);
-    cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear partition cursors");
+    u32 parts = 0;
+    u64 slots = 0;
+    size_t table_bytes, region_bytes = 0;
+    if (partition) {
+      const u64 parts64 = std::max<u64>(1, (u64)((double)so.terms / mean) + 1);
+      if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
+      parts = (u32)parts64;
+      region_bytes = (size_t)parts * pcap * candidate_bytes(p.R);
+      table_bytes = region_bytes + ((size_t)parts * 4 + 255) / 256 * 256;
+    } else {
+      slots = pow2_at_least(std::max<u64>(1024, so.terms * 2));
+      table_bytes = slots * slot_bytes(p.key_bits, p.R);
+    }
+    const u64 need_cap = final_step ? n_in : std::max<u64>(n_in, so.terms);
+    if (std::max<u64>(f.cap, need_cap) * eb + table_bytes > p.budget) {
+      if (n_in <= 1) fail(QPEPS_ERR_CAPACITY, row_msg("device budget exceeded at row", row + 1));
+      return StepStatus::NeedSplit;
+    }
+    if (ctx.table.bytes < table_bytes) buf_release(ctx, ctx.table);
+    if (f.cap < need_cap) {
+      if (ctx.pool_bytes + (need_cap - f.cap) * eb + table_bytes > p.budget) buf_release(ctx, ctx.table);
+      if (!ensure_front(ctx, p, f, need_cap, ctx.table.ptr ? 0 : table_bytes)) {
+        if (n_in <= 1) fail(QPEPS_ERR_CAPACITY, row_msg("device budget exceeded at row", row + 1));
+        return StepStatus::NeedSplit;
+      }
+    }
+    if (ctx.pool_bytes - ctx.table.bytes + table_bytes > p.budget) buf_release(ctx, ctx.table);
+    buf_reserve(ctx, ctx.table, table_bytes, p.budget, partition ? "partition regions" : "hash table");
+
+    LaunchCfg cfg{p.key_bits, p.R, p.threads, ctx.sms};
+    FrontierView view = view_of(p, ctx.front[0], f.cap);
+    const u64 terms = so.terms;
     cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-    FrontierView out{};
-    if (!final_step) out = view_of(p, ctx.front[1 - cur], out_cap);
-    PartitionCfg pc{p.R, ctx.sms, parts, cap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1};
+    PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1};
+    void* regions = ctx.table.ptr;
+    uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
+    if (partition)
+      cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear partition cursors");
+    else
+      cuda_check(cudaMemsetAsync(ctx.table.ptr, 0, table_bytes, ctx.stream), "clear hash table");
     cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
-    cuda_check(launch_partition_scatter(pc, in, n_in, p.n, regions, cursors, ctx.d_sc, ctx.stream),
-               "partition scatter kernel");
+    if (partition)
+      cuda_check(launch_partition_scatter(pc, view, n_in, p.n, regions, cursors, ctx.d_sc, ctx.stream),
+                 "partition scatter kernel");
+    else if (site)
+      cuda_check(launch_site_expand_insert(cfg, view, n_in, p.n, site_idx, ctx.table.ptr, slots, ctx.d_sc, ctx.stream),
+                 "site expand-insert kernel");
+    else
+      cuda_check(launch_row_expand_insert(cfg, view, n_in, p.n, ctx.table.ptr, slots, ctx.d_sc, ctx.stream),
+                 "row expand-insert kernel");
     cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
-    cuda_check(launch_partition_merge(pc, regions, cursors, out, p.n, !final_step, ctx.d_sc, ctx.stream),
-               "partition merge kernel");
+    if (partition)
+      cuda_check(launch_partition_merge_cluster(pc, regions, cursors, view, p.n, !final_step, ctx.d_sc, ctx.stream),
+                 "partition merge kernel");
+    else
+      cuda_check(launch_compact(cfg, ctx.table.ptr, slots, view, p.n, !final_step, ctx.d_sc, ctx.stream),
+                 "compact kernel");
     cuda_check(cudaEventRecord(ctx.ev[2], ctx.stream), "event");
     rs.launches += 2;
     sync_scalars(ctx);
-    if (ctx.h_sc->error & kErrOverflow) {
-      // A partition received more candidates than its slots: retry with
-      // smaller partitions (the scatter wrote nothing past a full partition).
+    if (partition && (ctx.h_sc->error & kErrOverflow)) {
+      // The merge kernel saw the flag and wrote nothing: the input is intact.
       if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, row_msg("partition overflow persists at row", row + 1));
       mean *= 0.6;
+      ctx.partition_fill = std::max(0.3, ctx.partition_fill * 0.8);  // keep a wider margin for this context
+      (void)terms;
       continue;
     }
+    if (ctx.h_sc->error & kErrProbeLimit) fail(QPEPS_ERR_CAPACITY, row_msg("hash probe bound exceeded at row", row + 1));
     if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, row_msg("device capacity error at row", row + 1));
-    float ms_scatter = 0, ms_merge = 0;
-    cudaEventElapsedTime(&ms_scatter, ctx.ev[0], ctx.ev[1]);
-    cudaEventElapsedTime(&ms_merge, ctx.ev[1], ctx.ev[2]);
+    float ms_a = 0, ms_b = 0;
+    cudaEventElapsedTime(&ms_a, ctx.ev[0], ctx.ev[1]);
+    cudaEventElapsedTime(&ms_b, ctx.ev[1], ctx.ev[2]);
     so.out = ctx.h_sc->out_count;
-    so.out_cap = out_cap;
     for (int r = 0; r < p.R; ++r) {
       so.weight[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
       so.final_sum[r] = ctx.h_sc->final_sum[r] % kPrimes[r];
     }
-    rs.device_ms += ms_scatter + ms_merge;
-    rs.merge_ms += ms_merge;
-    rs.scatter_ms += ms_scatter;
+    rs.device_ms += ms_a + ms_b;
+    rs.scatter_ms += ms_a;
+    rs.merge_ms += ms_b;
     rs.merge_launches += 1;
-    rs.merge_bytes += n_in * entry_bytes(p) + so.out * entry_bytes(p);
+    rs.merge_bytes += (n_in + so.out) * eb;
     rs.entries_in += n_in;
     rs.entries_out += so.out;
     rs.candidates += so.terms;
-    return so;
+    f.count = final_step ? 0 : so.out;
+    *so_out = so;
+    return StepStatus::Ok;
   }
 }
 
-static void upload_items(Ctx& ctx, const Plan& p, const std::vector<Item>& items, size_t lo, size_t hi, int buf,
-                         u64* cap_out) {
-  const u64 cnt = hi - lo;
-  const u64 cap = std::max<u64>(cnt, 1);
-  buf_reserve(ctx, ctx.front[buf], cap * entry_bytes(p), p.budget, "boundary buffer");
-  FrontierView v = view_of(p, ctx.front[buf], cap);
-  std::vector<uint8_t> keys(cap * (p.key_bits / 8));
-  std::vector<uint32_t> res((size_t)p.R * cap);
-  for (u64 i = 0; i < cnt; ++i) {
-    const Item& it = items[lo + i];
-    if (p.key_bits == 64) {
-      u64 k = (u64)it.key;
-      std::memcpy(&keys[i * 8], &k, 8);
-    } else {
-      std::memcpy(&keys[i * 16], &it.key, 16);
-    }
-    for (int r = 0; r < p.R; ++r) res[(size_t)r * cap + i] = (uint32_t)(it.weight % kPrimes[r]);
-  }
-  cuda_check(cudaMemcpyAsync(v.keys, keys.data(), keys.size(), cudaMemcpyHostToDevice, ctx.stream), "upload keys");
-  cuda_check(cudaMemcpyAsync(v.res, res.data(), res.size() * 4, cudaMemcpyHostToDevice, ctx.stream),
-             "upload residues");
-  cuda_check(cudaStreamSynchronize(ctx.stream), "upload synchronize");
-  *cap_out = cap;
+// Move the upper half of the live boundary to the host; the caller resumes it
+// later at the same (row, site).
+static void split_to_host(Ctx& ctx, const Plan& p, DevFrontier& f, unsigned row, unsigned site, bool row_counted,
+                          bool no_tail, std::vector<HostChunk>& pending) {
+  const u64 keep = f.count / 2, moved = f.count - keep;
+  HostChunk hc;
+  hc.row = row;
+  hc.site = site;
+  hc.row_counted = row_counted;
+  hc.no_tail = no_tail;
+  hc.count = moved;
+  const size_t kb = key_bytes(p);
+  hc.keys.resize(moved * kb);
+  hc.res.resize((size_t)p.R * moved);
+  const char* src = static_cast<const char*>(ctx.front[0].ptr);
+  cuda_check(cudaMemcpyAsync(hc.keys.data(), src + keep * kb, moved * kb, cudaMemcpyDeviceToHost, ctx.stream),
+             "spill keys");
+  for (int r = 0; r < p.R; ++r)
+    cuda_check(cudaMemcpyAsync(hc.res.data() + (size_t)r * moved, src + f.cap * kb + ((size_t)r * f.cap + keep) * 4,
+                               moved * 4, cudaMemcpyDeviceToHost, ctx.stream),
+               "spill residues");
+  cuda_check(cudaStreamSynchronize(ctx.stream), "spill synchronize");
+  f.count = keep;
+  pending.push_back(std::move(hc));
 }
 
-// Contract rows [row0, n) for items[lo, hi) as one merged device boundary.
-// Row metrics are added into `rows` only when the whole batch succeeds.
-static void run_batch(Ctx& ctx, const Plan& p, const std::vector<Item>& items, size_t lo, size_t hi, unsigned row0,
-                      std::vector<RowAcc>& rows, RunStats& rs, bool collect) {
-  RunStats local;
-  std::vector<RowAcc> lrows(p.n);
-  u64 cap = 0;
-  int cur = 0;
-  // Every pooled buffer is dead between batches: drop them if a previous,
-  // larger call left the pool above this call's budget.
-  if (ctx.pool_bytes > p.budget / 2) {
+static void upload_chunk(Ctx& ctx, const Plan& p, const HostChunk& hc, DevFrontier& f) {
+  // Pooled buffers are dead between chunks; drop them only if they exceed
+  // this call's budget or cannot hold the chunk.
+  f.count = 0;
+  if (ctx.pool_bytes > p.budget) buf_release(ctx, ctx.table);
+  if (f.cap < hc.count || ctx.front[0].bytes > p.budget) {
     buf_release(ctx, ctx.front[0]);
-    buf_release(ctx, ctx.front[1]);
-    buf_release(ctx, ctx.table);
+    f.cap = 0;
   }
-  upload_items(ctx, p, items, lo, hi, cur, &cap);
-  u64 count = hi - lo;
-  local.peak_states = count;
+  if (!ensure_front(ctx, p, f, std::max<u64>(hc.count, 1), 0))
+    fail(QPEPS_ERR_CAPACITY, "device budget cannot hold the seed boundary");
+  const size_t kb = key_bytes(p);
+  char* dst = static_cast<char*>(ctx.front[0].ptr);
+  cuda_check(cudaMemcpyAsync(dst, hc.keys.data(), hc.count * kb, cudaMemcpyHostToDevice, ctx.stream), "upload keys");
+  for (int r = 0; r < p.R; ++r)
+    cuda_check(cudaMemcpyAsync(dst + f.cap * kb + (size_t)r * f.cap * 4, hc.res.data() + (size_t)r * hc.count,
+                               hc.count * 4, cudaMemcpyHostToDevice, ctx.stream),
+               "upload residues");
+  cuda_check(cudaStreamSynchronize(ctx.stream), "upload synchronize");
+  f.count = hc.count;
+}
+
+static HostChunk chunk_from_items(const Plan& p, const std::vector<Item>& items, unsigned row) {
+  HostChunk hc;
+  hc.row = row;
+  hc.count = items.size();
+  const size_t kb = key_bytes(p);
+  hc.keys.resize(hc.count * kb);
+  hc.res.resize((size_t)p.R * hc.count);
+  for (u64 i = 0; i < hc.count; ++i) {
+    if (kb == 8) {
+      const u64 k = (u64)items[i].key;
+      std::memcpy(&hc.keys[i * 8], &k, 8);
+    } else {
+      std::memcpy(&hc.keys[i * 16], &items[i].key, 16);
+    }
+    for (int r = 0; r < p.R; ++r) hc.res[(size_t)r * hc.count + i] = (uint32_t)(items[i].weight % kPrimes[r]);
+  }
+  return hc;
+}
+
+// Rows [row0, n) of every live boundary entry through the slice-tail kernel;
+// entries that overflow its shared-memory capacity come back as a host chunk
+// that the row engine contracts to the end.
+static void run_tail(Ctx& ctx, const Plan& p, DevFrontier& f, unsigned row0, std::vector<RowAcc>& rows, RunStats& rs,
+                     std::vector<HostChunk>& pending) {
+  const u64 items = f.count;
+  const size_t ctl_bytes = (sizeof(TailControl) + 255) / 256 * 256;
+  const size_t need = ctl_bytes + items * 8;
+  if (ctx.tail.bytes < need) {
+    buf_release(ctx, ctx.tail);
+    if (ctx.pool_bytes + need > p.budget) buf_release(ctx, ctx.table);
+    buf_reserve(ctx, ctx.tail, need, p.budget, "slice-tail control");
+  }
+  TailControl* d_ctl = static_cast<TailControl*>(ctx.tail.ptr);
+  uint64_t* d_over = reinterpret_cast<uint64_t*>(static_cast<char*>(ctx.tail.ptr) + ctl_bytes);
+  TailControl h{};
+  h.overflow_cap = items;
+  h.overflow_items = d_over;
+  cuda_check(cudaMemcpyAsync(d_ctl, &h, sizeof h, cudaMemcpyHostToDevice, ctx.stream), "tail control");
+  FrontierView view = view_of(p, ctx.front[0], f.cap);
+  const auto t0 = std::chrono::steady_clock::now();
+  cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+  cuda_check(launch_slice_tail(p.R, view, items, p.n, row0, d_ctl, ctx.sms, ctx.stream), "slice tail kernel");
+  cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+  rs.launches += 1;
+  cuda_check(cudaMemcpyAsync(&h, d_ctl, sizeof h, cudaMemcpyDeviceToHost, ctx.stream), "tail results");
+  cuda_check(cudaStreamSynchronize(ctx.stream), "tail synchronize");
+  if (h.error) fail(QPEPS_ERR_CAPACITY, "slice-tail overflow list exceeded");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
+  rs.tail_ms += ms;
+  rs.device_ms += ms;
+  rs.tail_items += items;
+  rs.tail_overflow += h.overflow_count;
+  for (int r = 0; r < p.R; ++r) rs.final_res[r] = (rs.final_res[r] + h.final_sum[r] % kPrimes[r]) % kPrimes[r];
+  const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   for (unsigned row = row0; row < p.n; ++row) {
-    auto t0 = std::chrono::steady_clock::now();
-    const bool last_row = row + 1 == p.n;
-    RowAcc& acc = lrows[row];
+    const unsigned q = row - row0;
+    RowAcc& acc = rows[row];
     acc.used = true;
     acc.device_row = true;
-    acc.input_states = count;
-    acc.candidates = (u128)count * p.n;
-    StepOut so{};
-    if (p.grain == QPEPS_GRAIN_SITE) {
-      // Row-level successor count for the metrics (compiled-operator view).
-      LaunchCfg cfg{p.key_bits, p.R, p.threads, ctx.sms};
-      cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-      cuda_check(launch_row_count(cfg, view_of(p, ctx.front[cur], cap), count, p.n, ctx.d_sc, ctx.stream),
-                 "row count kernel");
-      local.launches += 1;
-      sync_scalars(ctx);
-      const u64 row_terms = ctx.h_sc->terms;
-      for (unsigned site = 0; site < p.n; ++site) {
-        const bool fin = last_row && site + 1 == p.n;
-        so = merge_step(ctx, p, cur, count, cap, true, site, fin, local, row);
-        count = so.out;
-        if (!fin) {
-          cur = 1 - cur;
-          cap = so.out_cap;
+    acc.input_states += h.row_acc[q][0];
+    acc.output_states += h.row_acc[q][1];
+    acc.matched += h.row_acc[q][2];
+    acc.completed += h.row_acc[q][2];
+    acc.candidates += (u128)h.row_acc[q][0] * p.n;
+    for (int r = 0; r < p.R; ++r) acc.weight_res[r] = (acc.weight_res[r] + h.row_acc[q][3 + r] % kPrimes[r]) % kPrimes[r];
+    acc.elapsed += el / (p.n - row0);
+    rs.entries_in += h.row_acc[q][0];
+    rs.entries_out += h.row_acc[q][1];
+    rs.candidates += h.row_acc[q][2];
+  }
+  if (h.overflow_count) {
+    // Gather the overflowing entries (compact, plane stride = count) into the
+    // table buffer, then park them on the host as a merged chunk.
+    const u64 m = h.overflow_count;
+    const size_t kb = key_bytes(p);
+    const size_t bytes = m * (kb + 4u * p.R);
+    if (ctx.table.bytes < bytes) {
+      buf_release(ctx, ctx.table);
+      buf_reserve(ctx, ctx.table, bytes, p.budget, "tail overflow gather");
+    }
+    uint64_t* gk = static_cast<uint64_t*>(ctx.table.ptr);
+    uint32_t* gr = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + m * kb);
+    cuda_check(launch_gather_entries(p.R, view, d_over, m, gk, gr, ctx.sms, ctx.stream), "gather kernel");
+    rs.launches += 1;
+    HostChunk hc;
+    hc.row = row0;
+    hc.no_tail = true;
+    hc.count = m;
+    hc.keys.resize(m * kb);
+    hc.res.resize((size_t)p.R * m);
+    cuda_check(cudaMemcpyAsync(hc.keys.data(), gk, m * kb, cudaMemcpyDeviceToHost, ctx.stream), "overflow keys");
+    cuda_check(cudaMemcpyAsync(hc.res.data(), gr, m * 4u * p.R, cudaMemcpyDeviceToHost, ctx.stream),
+               "overflow residues");
+    cuda_check(cudaStreamSynchronize(ctx.stream), "overflow synchronize");
+    pending.push_back(std::move(hc));
+  }
+  f.count = 0;
+}
+
+// Contract every pending chunk to the last row. Each chunk is one merged
+// device boundary; under memory pressure a boundary is halved and the upper
+// half parked on the host (exact: the contraction is linear in the boundary).
+static void run_chunks(Ctx& ctx, const Plan& p, std::vector<HostChunk> pending, std::vector<RowAcc>& rows,
+                       RunStats& rs) {
+  DevFrontier f;
+  buf_release(ctx, ctx.front[1]);
+  // The boundary buffer persists across calls; its plane stride follows this
+  // plan's entry size.
+  f.cap = ctx.front[0].ptr ? ctx.front[0].bytes / entry_bytes(p) : 0;
+  while (!pending.empty()) {
+    HostChunk hc = std::move(pending.back());
+    pending.pop_back();
+    upload_chunk(ctx, p, hc, f);
+    rs.batches += 1;
+    rs.peak_states = std::max<u64>(rs.peak_states, f.count);
+    unsigned site0 = hc.site;
+    bool counted = hc.row_counted;
+    const unsigned stop = hc.no_tail ? p.n : std::max(p.tail_row, hc.row);
+    for (unsigned row = hc.row; row < stop; ++row) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const bool last_row = row + 1 == p.n;
+      RowAcc& acc = rows[row];
+      acc.used = true;
+      acc.device_row = true;
+      StepOut so;
+      if (p.grain == QPEPS_GRAIN_SITE) {
+        if (!counted) {
+          const u64 row_terms = count_terms(ctx, p, f, false, 0, rs);
+          acc.input_states += f.count;
+          acc.candidates += (u128)f.count * p.n;
+          acc.matched += row_terms;
+          acc.completed += row_terms;
         }
+        for (unsigned site = site0; site < p.n; ++site) {
+          const bool fin = last_row && site + 1 == p.n;
+          while (merge_step(ctx, p, f, true, site, fin, rs, row, &so) == StepStatus::NeedSplit)
+            split_to_host(ctx, p, f, row, site, true, hc.no_tail, pending);
+          if (fin)
+            for (int r = 0; r < p.R; ++r) rs.final_res[r] = (rs.final_res[r] + so.final_sum[r]) % kPrimes[r];
+        }
+        site0 = 0;
+        counted = false;
+      } else {
+        while (merge_step(ctx, p, f, false, 0, last_row, rs, row, &so) == StepStatus::NeedSplit)
+          split_to_host(ctx, p, f, row, 0, false, hc.no_tail, pending);
+        acc.input_states += so.in;
+        acc.candidates += (u128)so.in * p.n;
+        acc.matched += so.terms;
+        acc.completed += so.terms;
+        if (last_row)
+          for (int r = 0; r < p.R; ++r) rs.final_res[r] = (rs.final_res[r] + so.final_sum[r]) % kPrimes[r];
       }
-      acc.matched = acc.completed = row_terms;
-    } else {
-      so = p.merge == QPEPS_MERGE_PARTITION ? merge_step_partition(ctx, p, cur, count, cap, last_row, local, row)
-                                            : merge_step(ctx, p, cur, count, cap, false, 0, last_row, local, row);
-      count = so.out;
-      if (!last_row) {
-        cur = 1 - cur;
-        cap = so.out_cap;
-      }
-      acc.matched = acc.completed = so.terms;
+      acc.output_states += last_row ? so.out : f.count;
+      for (int r = 0; r < p.R; ++r) acc.weight_res[r] = (acc.weight_res[r] + so.weight[r]) % kPrimes[r];
+      rs.peak_states = std::max<u64>(rs.peak_states, last_row ? so.out : f.count);
+      acc.elapsed += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
-    acc.output_states = count;
-    for (int r = 0; r < p.R; ++r) acc.weight_res[r] = so.weight[r];
-    local.peak_states = std::max<u64>(local.peak_states, count);
-    if (last_row)
-      for (int r = 0; r < p.R; ++r) local.final_res[r] = so.final_sum[r];
-    acc.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    if (count == 0 && !last_row) {
-      // Empty boundary: nothing can complete; remaining rows see no input.
-      for (unsigned r2 = row + 1; r2 < p.n; ++r2) {
-        lrows[r2].used = true;
-        lrows[r2].device_row = true;
-      }
-      break;
-    }
+    if (stop < p.n && f.count > 0) run_tail(ctx, p, f, stop, rows, rs, pending);
   }
-  (void)collect;
-  // Commit.
-  for (unsigned row = 0; row < p.n; ++row) {
-    if (!lrows[row].used) continue;
-    RowAcc& a = rows[row];
-    a.used = true;
-    a.device_row = a.device_row || lrows[row].device_row;
-    a.input_states += lrows[row].input_states;
-    a.output_states += lrows[row].output_states;
-    a.candidates += lrows[row].candidates;
-    a.matched += lrows[row].matched;
-    a.completed += lrows[row].completed;
-    for (int r = 0; r < p.R; ++r) a.weight_res[r] = (a.weight_res[r] + lrows[row].weight_res[r]) % kPrimes[r];
-    a.elapsed += lrows[row].elapsed;
-  }
-  for (int r = 0; r < p.R; ++r) rs.final_res[r] = (rs.final_res[r] + local.final_res[r]) % kPrimes[r];
-  rs.entries_in += local.entries_in;
-  rs.entries_out += local.entries_out;
-  rs.candidates += local.candidates;
-  rs.launches += local.launches;
-  rs.device_ms += local.device_ms;
-  rs.merge_ms += local.merge_ms;
-  rs.scatter_ms += local.scatter_ms;
-  rs.merge_launches += local.merge_launches;
-  rs.merge_bytes += local.merge_bytes;
-  rs.peak_states = std::max(rs.peak_states, local.peak_states);
-  rs.batches += 1;
 }
 
 // Host expansion of one row over a merged item list (used for the first
@@ -758,75 +882,31 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o) {
     p.merge = partition_ok ? QPEPS_MERGE_PARTITION : QPEPS_MERGE_HASH;
   else
     fail(QPEPS_ERR_INVALID, "unknown merge strategy");
+  // The slice tail needs u64 keys and the compiled row operator.
+  const bool tail_ok = p.key_bits == 64 && p.grain == QPEPS_GRAIN_ROW && n >= 2;
+  if (o.tail_row == 0)
+    p.tail_row = n;  // auto: the merged row engine for every row (fastest measured through N=18)
+  else
+    p.tail_row = (tail_ok && o.tail_row < n) ? o.tail_row : n;
   return p;
 }
 
 // Contract rows from a list of seed items at depth row0 (rows already applied).
-static void contract_items(Ctx& ctx, Contraction& out, std::vector<Item> items, unsigned row0) {
+static void contract_items(Ctx& ctx, Contraction& out, const std::vector<Item>& items, unsigned row0) {
   const Plan& p = out.plan;
-  // Batches: start with everything merged; on a capacity failure split the
-  // batch in halves; a single item that still does not fit is deepened by one
-  // host row into child items.
-  struct Range {
-    size_t lo, hi;
-    unsigned depth;
-    std::vector<Item>* src;
-  };
-  std::vector<std::vector<Item>*> owned;
-  std::vector<Range> work;
-  if (!items.empty()) {
-    owned.push_back(new std::vector<Item>(std::move(items)));
-    work.push_back(Range{0, owned.back()->size(), row0, owned.back()});
+  if (items.empty()) return;
+  if (row0 >= p.n) {
+    // Fully placed boards.
+    const u64 mask = (p.n >= 64) ? ~0ull : ((1ull << p.n) - 1);
+    for (const Item& it : items)
+      if (((u64)it.key & mask) == mask)
+        for (int r = 0; r < p.R; ++r)
+          out.rs.final_res[r] = (out.rs.final_res[r] + (u64)(it.weight % kPrimes[r])) % kPrimes[r];
+    return;
   }
-  try {
-    while (!work.empty()) {
-      Range w = work.back();
-      work.pop_back();
-      if (w.depth >= p.n) {
-        // Fully placed: every item is a finished board.
-        const u64 mask = (p.n >= 64) ? ~0ull : ((1ull << p.n) - 1);
-        for (size_t i = w.lo; i < w.hi; ++i) {
-          const Item& it = (*w.src)[i];
-          if (((u64)it.key & mask) == mask)
-            for (int r = 0; r < p.R; ++r)
-              out.rs.final_res[r] = (out.rs.final_res[r] + (u64)(it.weight % kPrimes[r])) % kPrimes[r];
-        }
-        continue;
-      }
-      try {
-        run_batch(ctx, p, *w.src, w.lo, w.hi, w.depth, out.rows, out.rs, true);
-      } catch (const Failure& f) {
-        if (f.code != QPEPS_ERR_CAPACITY) throw;
-        if (w.hi - w.lo > 1) {
-          const size_t mid = w.lo + (w.hi - w.lo) / 2;
-          work.push_back(Range{mid, w.hi, w.depth, w.src});
-          work.push_back(Range{w.lo, mid, w.depth, w.src});
-        } else {
-          RowAcc scratch;
-          std::vector<Item> one{(*w.src)[w.lo]};
-          owned.push_back(new std::vector<Item>(host_expand(p.n, one, w.depth, false, scratch)));
-          if (owned.back()->empty()) continue;
-          out.slice_depth = std::max(out.slice_depth, w.depth + 1);
-          // The host row is not a device row; its metrics are folded in.
-          RowAcc& a = out.rows[w.depth];
-          a.used = true;
-          a.input_states += scratch.input_states;
-          a.output_states += scratch.output_states;
-          a.candidates += scratch.candidates;
-          a.matched += scratch.matched;
-          a.completed += scratch.completed;
-          for (int r = 0; r < p.R; ++r)
-            a.weight_res[r] = (a.weight_res[r] + (u64)(scratch.weight_exact % kPrimes[r])) % kPrimes[r];
-          a.device_row = true;
-          work.push_back(Range{0, owned.back()->size(), w.depth + 1, owned.back()});
-        }
-      }
-    }
-  } catch (...) {
-    for (auto* v : owned) delete v;
-    throw;
-  }
-  for (auto* v : owned) delete v;
+  std::vector<HostChunk> pending;
+  pending.push_back(chunk_from_items(p, items, row0));
+  run_chunks(ctx, p, std::move(pending), out.rows, out.rs);
 }
 
 static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
@@ -885,7 +965,7 @@ static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_
     ++row0;
   }
   out.slice_depth = row0;
-  contract_items(ctx, out, std::move(items), row0);
+  contract_items(ctx, out, items, row0);
   out.peak_states = std::max<u64>(out.peak_states, out.rs.peak_states);
   // Count: host-finished boards plus device final sums, then CRT.
   u64 res[kMaxResidues];
@@ -954,6 +1034,10 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->scatter_kernel_ms = c.rs.scatter_ms;
   r->merge_kernel_launches = c.rs.merge_launches;
   r->merge_kernel_bytes = c.rs.merge_bytes;
+  r->tail_row = n ? c.plan.tail_row : 0;
+  r->tail_items = c.rs.tail_items;
+  r->tail_overflow = c.rs.tail_overflow;
+  r->tail_kernel_ms = c.rs.tail_ms;
   for (int i = 0; i < kMaxResidues; ++i) {
     r->residue_primes[i] = i < (n ? c.plan.R : 0) ? kPrimes[i] : 0;
     r->count_residues[i] = i < (n ? c.plan.R : 0) ? (uint64_t)(c.count % kPrimes[i]) : 0;

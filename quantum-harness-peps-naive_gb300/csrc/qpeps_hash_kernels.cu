@@ -252,6 +252,7 @@ __global__ void __launch_bounds__(BLOCK) compact_kernel(const Slot<K, R>* __rest
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const u64 mask = board_mask(n);
   const u64 chunk = (u64)BLOCK * ITEMS;
+  if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;  // insertion failed: leave the boundary intact
   unsigned long long wsum[R], fsum[R], fstates = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;

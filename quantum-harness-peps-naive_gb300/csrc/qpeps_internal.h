@@ -91,4 +91,36 @@ cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, 
                                    const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
                                    cudaStream_t stream);
 
+// Merge through a 4-CTA cluster sharing a distributed shared-memory table;
+// partitions hold cluster_partition_capacity() candidates.
+uint32_t cluster_partition_capacity();
+cudaError_t launch_partition_merge_cluster(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                                           const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
+                                           cudaStream_t stream);
+
+// Slice-tail kernel control block (device memory). Row statistics per tail
+// row q (row0 + q): [0] input states, [1] output states, [2] successor terms,
+// [3 + r] output weight residue r.
+constexpr int kTailMaxRows = 32;
+constexpr int kTailRowFields = 7;
+struct TailControl {
+  unsigned long long next_item;
+  unsigned long long overflow_count;
+  unsigned long long overflow_cap;
+  uint64_t* overflow_items;
+  unsigned long long final_sum[4];
+  unsigned long long row_acc[kTailMaxRows][kTailRowFields];
+  unsigned int error;
+  unsigned int pad[3];
+};
+
+// Contract rows [row0, n) of every boundary entry independently, one warp per
+// entry, in shared memory. Entries whose frontier exceeds tail_capacity()
+// states are listed in ctl->overflow_items.
+uint32_t tail_capacity();
+cudaError_t launch_gather_entries(int residues, const FrontierView& in, const uint64_t* idx, uint64_t m,
+                                  uint64_t* out_keys, uint32_t* out_res, int sms, cudaStream_t stream);
+cudaError_t launch_slice_tail(int residues, const FrontierView& in, uint64_t n_items, unsigned n, unsigned row0,
+                              TailControl* ctl, int sms, cudaStream_t stream);
+
 }  // namespace qpeps

@@ -13,6 +13,7 @@
 // This replaces the reference's `candidates.sort_unstable_by_key` + checked
 // reduce (src/lib.rs:5353-5367): equal packed keys are merged by addition;
 // the order of the output boundary is not observable by any metric.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "qpeps_device.cuh"
@@ -237,6 +238,10 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   __shared__ unsigned long long s_base;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const u64 mask = pboard_mask(n);
+  // A partition overflowed in the scatter: write nothing, so the boundary
+  // buffer (read by the scatter, written here in place) stays intact for the
+  // host's retry with smaller partitions.
+  if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
   unsigned long long wsum[R], fsum[R], fstates = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
@@ -355,6 +360,165 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
 }
 
+// ---------------------------------------------------------------------------
+// Cluster merge. A thread-block cluster of CL CTAs shares one distributed
+// shared-memory table of CL*H slots (each CTA owns H), so one partition can
+// hold CL*H/2 candidates. Bigger partitions mean fewer open partition tails
+// for the scatter (they must stay in L2 for its 16-byte stores to be
+// write-combined). Each CTA loads a quarter of the partition, inserts every
+// candidate into its home CTA's table with DSMEM atomics (home and slot come
+// from the low hash bits, independent of the high bits that chose the
+// partition), and after a cluster barrier compacts and resets its own table.
+
+template <int R, int BLOCK, int H, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BLOCK)
+    partition_merge_cluster_kernel(const Cand<R>* __restrict__ regions, const u32* __restrict__ cursors, u32 parts,
+                                   u64* __restrict__ keys_out, u32* __restrict__ res_out, u64 out_stride, unsigned n,
+                                   int write_out, StepScalars* __restrict__ sc) {
+  namespace cg = cooperative_groups;
+  constexpr int WARPS = BLOCK / 32;
+  constexpr int PER = H / BLOCK;
+  constexpr int CAP = CL * H / 2;
+  constexpr int SLICE = CAP / CL;
+  constexpr int LPT = SLICE / BLOCK;
+  static_assert(H % BLOCK == 0 && SLICE % BLOCK == 0 && PER <= 32 && (PER * WARPS) % 32 == 0, "shape");
+  static_assert((CL & (CL - 1)) == 0 && (H & (H - 1)) == 0, "power-of-two cluster and table");
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u64* s_key = reinterpret_cast<u64*>(smem_raw);
+  unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [R][H]
+  __shared__ u32 s_cnt[PER * WARPS];
+  __shared__ unsigned long long s_base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const u64 mask = pboard_mask(n);
+  if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;  // uniform across the cluster
+  unsigned long long wsum[R], fsum[R], fstates = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
+  for (int i = threadIdx.x; i < H; i += BLOCK) {
+    s_key[i] = kEmpty;
+#pragma unroll
+    for (int r = 0; r < R; ++r) s_acc[r * H + i] = 0ull;
+  }
+  u64* rkey[CL];
+  unsigned long long* racc[CL];
+#pragma unroll
+  for (int c = 0; c < CL; ++c) {
+    rkey[c] = cluster.map_shared_rank(s_key, c);
+    racc[c] = cluster.map_shared_rank(s_acc, c);
+  }
+  const u32 cid = blockIdx.x / CL, ncl = gridDim.x / CL;
+  Cand<R> buf[LPT];
+  u32 bcnt = 0;
+  auto fetch = [&](u32 part) {
+    bcnt = min(cursors[part], (u32)CAP);
+    const Cand<R>* src = regions + (u64)part * CAP;
+#pragma unroll
+    for (int l = 0; l < LPT; ++l) {
+      const u32 i = rank * SLICE + l * BLOCK + threadIdx.x;
+      if (i < bcnt) buf[l] = load_cand<R>(src + i);
+    }
+  };
+  u32 part = cid;
+  if (part < parts) fetch(part);
+  cluster.sync();
+  for (; part < parts; part += ncl) {
+#pragma unroll
+    for (int l = 0; l < LPT; ++l) {
+      const u32 i = rank * SLICE + l * BLOCK + threadIdx.x;
+      if (i < bcnt) {
+        const Cand<R>& c = buf[l];
+        const u64 h = mix64(c.key);
+        const int home = (int)(h & (CL - 1));
+        u64* tk = rkey[home];
+        unsigned long long* ta = racc[home];
+        u32 slot = (u32)(h >> 8) & (H - 1);
+        for (int probe = 0; probe < H; ++probe) {
+          u64 cur = tk[slot];
+          if (cur == kEmpty) {
+            cur = atomicCAS(reinterpret_cast<unsigned long long*>(&tk[slot]), kEmpty, c.key);
+            if (cur == kEmpty) cur = c.key;
+          }
+          if (cur == c.key) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) atomicAdd(&ta[r * H + slot], (unsigned long long)c.res[r]);
+            break;
+          }
+          slot = (slot + 1) & (H - 1);
+        }
+      }
+    }
+    cluster.sync();
+    const u32 next = part + ncl;
+    if (next < parts) fetch(next);
+    u32 flags = 0;
+#pragma unroll
+    for (int it = 0; it < PER; ++it) {
+      const bool occ = s_key[it * BLOCK + threadIdx.x] != kEmpty;
+      flags |= (u32)occ << it;
+      const u32 b = __ballot_sync(kFullMask, occ);
+      if (lane == 0) s_cnt[it * WARPS + wid] = __popc(b);
+    }
+    __syncthreads();
+    if (wid == 0) {
+      constexpr int PL = PER * WARPS / 32;
+      u32 v[PL];
+      u32 sum = 0;
+#pragma unroll
+      for (int q = 0; q < PL; ++q) {
+        v[q] = s_cnt[lane * PL + q];
+        sum += v[q];
+      }
+      const int incl = pwarp_inclusive_scan((int)sum);
+      u32 run = (u32)incl - sum;
+#pragma unroll
+      for (int q = 0; q < PL; ++q) {
+        s_cnt[lane * PL + q] = run;
+        run += v[q];
+      }
+      const int tot = __shfl_sync(kFullMask, incl, 31);
+      if (lane == 0) s_base = tot ? atomicAdd(&sc->out_count, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    const unsigned long long base = s_base;
+#pragma unroll
+    for (int it = 0; it < PER; ++it) {
+      const bool occ = (flags >> it) & 1u;
+      const u32 b = __ballot_sync(kFullMask, occ);
+      if (occ) {
+        const int slot = it * BLOCK + threadIdx.x;
+        const u64 key = s_key[slot];
+        const u64 idx = base + s_cnt[it * WARPS + wid] + __popc(b & ((1u << lane) - 1u));
+        const bool full = (key & mask) == mask;
+        if (write_out) keys_out[idx] = key;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const u32 v = (u32)(s_acc[r * H + slot] % prime_at(r));
+          if (write_out) res_out[r * out_stride + idx] = v;
+          wsum[r] += v;
+          if (full) fsum[r] += v;
+          s_acc[r * H + slot] = 0ull;
+        }
+        s_key[slot] = kEmpty;
+        fstates += full;
+      }
+    }
+    cluster.sync();  // tables reset before the cluster inserts the next partition
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    unsigned long long t = pblock_sum<BLOCK>(wsum[r]);
+    if (threadIdx.x == 0 && t) atomicAdd(&sc->weight_sum[r], t);
+    t = pblock_sum<BLOCK>(fsum[r]);
+    if (threadIdx.x == 0 && t) atomicAdd(&sc->final_sum[r], t);
+  }
+  const unsigned long long t = pblock_sum<BLOCK>(fstates);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+}
+
+constexpr int kClusterCTAs = 4;
+
 constexpr int kScatterBlock = 256;
 constexpr int kMergeBlock = 512;
 constexpr int kMergeH = 4096;
@@ -392,7 +556,38 @@ cudaError_t merge_impl(const PartitionCfg& pc, const void* regions, const u32* c
   return cudaGetLastError();
 }
 
+template <int R>
+cudaError_t merge_cluster_impl(const PartitionCfg& pc, const void* regions, const u32* cursors,
+                               const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
+                               cudaStream_t stream) {
+  auto kern = partition_merge_cluster_kernel<R, kMergeBlock, kMergeH, kClusterCTAs>;
+  const size_t smem = merge_smem<R>();
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const u64 clusters_cap = std::max<u64>(1, (u64)pc.sms * pc.merge_blocks_per_sm / kClusterCTAs);
+  const u64 clusters = std::max<u64>(1, std::min<u64>(pc.parts, clusters_cap));
+  kern<<<(unsigned)(clusters * kClusterCTAs), kMergeBlock, smem, stream>>>(
+      reinterpret_cast<const Cand<R>*>(regions), cursors, pc.parts, reinterpret_cast<u64*>(out.keys), out.res,
+      out.cap, n, write_out ? 1 : 0, sc);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+uint32_t cluster_partition_capacity() { return kClusterCTAs * kMergeH / 2; }
+
+cudaError_t launch_partition_merge_cluster(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                                           const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
+                                           cudaStream_t stream) {
+  if (pc.cap != cluster_partition_capacity()) return cudaErrorInvalidValue;
+  switch (pc.residues) {
+    case 1: return merge_cluster_impl<1>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 2: return merge_cluster_impl<2>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 3: return merge_cluster_impl<3>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 4: return merge_cluster_impl<4>(pc, regions, cursors, out, n, write_out, sc, stream);
+  }
+  return cudaErrorInvalidValue;
+}
 
 size_t candidate_bytes(int residues) { return residues <= 2 ? 16 : 32; }
 uint32_t partition_capacity() { return kMergeCap; }

@@ -203,3 +203,45 @@ def test_n16_hash_and_partition_agree(ctx, golden):
     assert a.count == b.count == 14772512
     assert [(l.output_states, l.output_weight) for l in a.layers] == [(l.output_states, l.output_weight) for l in b.layers]
     assert b.peak_states == golden["e36_orbit_n16"]["16"]["peak_support"]
+
+
+@pytest.mark.parametrize("n,k", [(6, 3), (8, 4), (10, 5), (12, 6), (13, 9), (14, 7)])
+def test_slice_tail_is_exact(ctx, oracle, n, k):
+    g = ctx.contract_rows(n, tail_row=k)
+    assert g.device["tail_row"] == k
+    assert g.count == oracle.known_count(n)
+    o = oracle.contract(n)
+    # Rows before the tail are the merged reference frontier.
+    assert _gpu_layers(g)[:k] == _oracle_layers(o)[:k]
+
+
+@pytest.mark.parametrize("n,k", [(10, 5), (12, 6), (13, 7), (14, 10)])
+def test_slice_tail_row_statistics(ctx, oracle, n, k):
+    # Row weights are linear in the boundary, so every tail row's output weight
+    # equals the merged reference's; the first tail row reads exactly the
+    # merged row-k boundary; later tail rows read at least the merged states
+    # (independent batches merge less).
+    g = ctx.contract_rows(n, tail_row=k)
+    o = oracle.contract(n)
+    assert [l.output_weight for l in g.layers] == [l["output_weight"] for l in o["layers"]]
+    assert g.layers[k].input_states == o["layers"][k]["input_states"]
+    assert g.layers[k].completed_row_terms == o["layers"][k]["completed_row_terms"]
+    for row in range(k + 1, n):
+        assert g.layers[row].input_states >= o["layers"][row]["input_states"]
+
+
+@pytest.mark.parametrize("n,k", [(12, 2), (14, 2), (15, 3)])
+def test_slice_tail_overflow_falls_back_to_row_engine(ctx, oracle, n, k):
+    # Entries this early have frontiers far beyond one warp's shared memory:
+    # they overflow and are contracted by the merged row engine instead.
+    g = ctx.contract_rows(n, tail_row=k)
+    assert g.device["tail_overflow"] > 0
+    assert g.count == oracle.known_count(n)
+
+
+def test_slice_tail_at_n17(ctx, oracle):
+    g = ctx.contract_rows(17, tail_row=9)
+    assert g.device["tail_row"] == 9 and g.device["tail_items"] > 0
+    assert g.count == oracle.known_count(17)
+    merged = ctx.contract_rows(17)
+    assert merged.device["tail_row"] == 17 and merged.count == g.count
