@@ -171,6 +171,46 @@ int qpeps_count_batch(void* ctx, uint32_t num, const uint32_t* n, const uint32_t
  * own C. */
 int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len);
 
+/* ---- Serving: continuous batching of counting requests -------------------
+ * No single reference counterpart: each request is the prefix contraction of
+ * qpeps_count (contract_rows, src/lib.rs:758, from a placed prefix). A server
+ * owns two contexts on one device: a shared batch where admitted requests of
+ * mixed N (<= 19) advance one row per step together, and a context that runs
+ * requests too large for the batch one at a time; both run concurrently.
+ * submit() never blocks on the GPU; poll() returns finished requests. */
+typedef struct qpeps_serve_config {
+  uint32_t struct_size;            /* sizeof(qpeps_serve_config) */
+  uint32_t max_slots;              /* concurrent requests in the shared batch (<= 64; 0 = 64) */
+  uint64_t batch_budget_bytes;     /* device memory of the shared batch (0 = 25 % of free) */
+  uint64_t large_budget_bytes;     /* device memory of the large-request context (0 = 60 % of free) */
+  uint64_t large_threshold_states; /* estimated peak frontier above which a request runs alone (0 = auto) */
+  uint32_t use_cache;              /* 1 = answer repeated (N, prefix or its mirror) from a result cache */
+  uint32_t reserved;
+} qpeps_serve_config;
+
+typedef struct qpeps_serve_completion {
+  uint64_t tag;
+  qpeps_u128 count;
+  int32_t status;   /* QPEPS_OK or an error code */
+  uint32_t n, k;
+  uint32_t path;    /* 0 shared batch, 1 large-request context, 2 result cache, 3 host (trivial prefix) */
+  double latency_s; /* submit -> completion */
+  double queue_s;   /* submit -> admission */
+} qpeps_serve_completion;
+
+typedef struct qpeps_serve_stats {
+  uint64_t submitted, completed, batch_steps, cache_hits, large_runs;
+} qpeps_serve_stats;
+
+void qpeps_serve_config_default(qpeps_serve_config* cfg);
+int qpeps_serve_open(int device, const qpeps_serve_config* cfg, void** server_out, char* err, size_t err_len);
+int qpeps_serve_submit(void* server, uint32_t n, const uint32_t* prefix, uint32_t k, uint64_t tag, char* err,
+                       size_t err_len);
+/* Copy up to `cap` completions into `out`; waits up to `wait_ms` when none is ready. */
+int qpeps_serve_poll(void* server, qpeps_serve_completion* out, uint32_t cap, uint32_t* got, uint32_t wait_ms);
+int qpeps_serve_stats_get(void* server, qpeps_serve_stats* out);
+void qpeps_serve_close(void* server);
+
 /* One row step of the partitioned merge that allocates no device memory.
  * No counterpart in the reference (its Rust driver owns all memory).
  *

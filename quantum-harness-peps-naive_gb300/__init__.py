@@ -121,6 +121,35 @@ class Options(ctypes.Structure):
     ]
 
 
+class ServeConfig(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("max_slots", ctypes.c_uint32),
+        ("batch_budget_bytes", ctypes.c_uint64),
+        ("large_budget_bytes", ctypes.c_uint64),
+        ("large_threshold_states", ctypes.c_uint64),
+        ("use_cache", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+    ]
+
+
+class ServeCompletion(ctypes.Structure):
+    _fields_ = [
+        ("tag", ctypes.c_uint64),
+        ("count", U128),
+        ("status", ctypes.c_int32),
+        ("n", ctypes.c_uint32),
+        ("k", ctypes.c_uint32),
+        ("path", ctypes.c_uint32),
+        ("latency_s", ctypes.c_double),
+        ("queue_s", ctypes.c_double),
+    ]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("submitted", "completed", "batch_steps", "cache_hits", "large_runs")]
+
+
 # Every symbol include/qpeps.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 _SIGNATURES = {
@@ -151,6 +180,21 @@ _SIGNATURES = {
          ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
          ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "qpeps_serve_config_default": (None, [ctypes.POINTER(ServeConfig)]),
+    "qpeps_serve_open": (
+        ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ServeConfig), ctypes.POINTER(_VP), ctypes.c_char_p, ctypes.c_size_t]
+    ),
+    "qpeps_serve_submit": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_uint64, ctypes.c_char_p,
+         ctypes.c_size_t],
+    ),
+    "qpeps_serve_poll": (
+        ctypes.c_int,
+        [_VP, ctypes.POINTER(ServeCompletion), ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32],
+    ),
+    "qpeps_serve_stats_get": (ctypes.c_int, [_VP, ctypes.POINTER(ServeStats)]),
+    "qpeps_serve_close": (None, [_VP]),
     "qpeps_certify_c": (
         ctypes.c_int,
         [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_char_p,
@@ -369,6 +413,81 @@ class Context:
             rc = lib.qpeps_count_batch(self._h, num, ns, ks, po, pc, ctypes.byref(o), counts, err, len(err))
         _check(rc, err)
         return [counts[i].value for i in range(num)]
+
+
+class Server:
+    """Continuous-batching counting server (qpeps_serve_*)."""
+
+    PATHS = {0: "batch", 1: "large", 2: "cache", 3: "host"}
+
+    def __init__(self, device: int = 0, **cfg):
+        lib = library()
+        c = ServeConfig()
+        lib.qpeps_serve_config_default(ctypes.byref(c))
+        for k, v in cfg.items():
+            if not hasattr(c, k) or k == "struct_size":
+                raise TypeError(f"unknown serve option {k}")
+            setattr(c, k, int(v))
+        err = ctypes.create_string_buffer(512)
+        h = _VP()
+        _check(lib.qpeps_serve_open(device, ctypes.byref(c), ctypes.byref(h), err, len(err)), err)
+        self._h = h
+
+    def submit(self, n: int, prefix: Sequence[int] = (), tag: int = 0) -> None:
+        k = len(prefix)
+        arr = (ctypes.c_uint32 * max(k, 1))(*prefix)
+        err = ctypes.create_string_buffer(512)
+        _check(library().qpeps_serve_submit(self._h, n, arr if k else None, k, tag, err, len(err)), err)
+
+    def poll(self, max_items: int = 1024, wait_ms: int = 0) -> list[dict]:
+        buf = (ServeCompletion * max_items)()
+        got = ctypes.c_uint32(0)
+        rc = library().qpeps_serve_poll(self._h, buf, max_items, ctypes.byref(got), wait_ms)
+        out = [
+            {"tag": b.tag, "count": b.count.value, "status": b.status, "n": b.n, "k": b.k,
+             "path": self.PATHS.get(b.path, b.path), "latency_s": b.latency_s, "queue_s": b.queue_s}
+            for b in buf[: got.value]
+        ]
+        if rc != QPEPS_OK:
+            raise ContractionError(rc, "server stopped")
+        return out
+
+    def stats(self) -> dict:
+        st = ServeStats()
+        library().qpeps_serve_stats_get(self._h, ctypes.byref(st))
+        return {f: getattr(st, f) for f, _ in ServeStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            library().qpeps_serve_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def random_prefix(rng, n: int, k: int) -> list[int]:
+    """k queens placed row by row, each column drawn uniformly from the
+    non-attacked columns of its row; the whole prefix is redrawn when a row has
+    no legal column."""
+    while True:
+        cols, dr, dl, out = 0, 0, 0, []
+        mask = (1 << n) - 1
+        ok = True
+        for _ in range(k):
+            free = [c for c in range(n) if not ((cols | dr | dl) >> c) & 1]
+            if not free:
+                ok = False
+                break
+            c = rng.choice(free)
+            b = 1 << c
+            cols, dr, dl = cols | b, ((dr | b) << 1) & mask, (dl | b) >> 1
+            out.append(c)
+        if ok:
+            return out
 
 
 _default_ctx: Context | None = None

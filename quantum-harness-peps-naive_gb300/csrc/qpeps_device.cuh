@@ -85,6 +85,55 @@ __host__ __device__ __forceinline__ K row_successor(const State& s, u64 bit, uns
   return pack<K>(s.cols | bit, ((s.dr | bit) << 1) & mask, (s.dl | bit) >> 1, n);
 }
 
+// ---- key layouts of the partitioned merge ----------------------------------
+//
+// FixedLayout: one board size, the reference's PackedBoundary bit layout.
+// SlotLayout: serving. Requests of different board sizes share one boundary;
+// each field is 19 bits wide (N <= 19) and bits [57, 63) hold the request's
+// slot, so entries of different requests never compare equal and never merge.
+// Bit 63 stays clear, keeping ~0 free as the empty-slot marker.
+
+struct FixedLayout {
+  static constexpr bool kSlotted = false;
+  unsigned n;
+  u64 mask;
+  __device__ __forceinline__ u64 mask_of(u64) const { return mask; }
+  __device__ __forceinline__ State unpack(u64 key) const { return qpeps::unpack<u64>(key, n, mask); }
+  __device__ __forceinline__ u64 successor(u64, const State& s, u64 bit) const {
+    return row_successor<u64>(s, bit, n, mask);
+  }
+  __device__ __forceinline__ unsigned slot(u64) const { return 0; }
+};
+
+constexpr unsigned kServeFieldBits = 19;
+constexpr unsigned kServeSlotShift = 57;
+constexpr unsigned kServeMaxSlots = 64;
+
+struct SlotLayout {
+  static constexpr bool kSlotted = true;
+  const u64* slot_mask;              // board mask per slot
+  unsigned long long* slot_final;    // [kServeMaxSlots][4] residue sums of finished boards
+  __device__ __forceinline__ u64 mask_of(u64 key) const { return slot_mask[key >> kServeSlotShift]; }
+  __device__ __forceinline__ State unpack(u64 key) const {
+    const u64 m = mask_of(key);
+    State s;
+    s.cols = key & m;
+    s.dr = (key >> kServeFieldBits) & m;
+    s.dl = (key >> (2 * kServeFieldBits)) & m;
+    return s;
+  }
+  __device__ __forceinline__ u64 successor(u64 key, const State& s, u64 bit) const {
+    const u64 m = mask_of(key);
+    return (key & (63ull << kServeSlotShift)) | (s.cols | bit) | ((((s.dr | bit) << 1) & m) << kServeFieldBits) |
+           (((s.dl | bit) >> 1) << (2 * kServeFieldBits));
+  }
+  __device__ __forceinline__ unsigned slot(u64 key) const { return (unsigned)(key >> kServeSlotShift); }
+};
+
+__host__ __device__ __forceinline__ u64 serve_key(unsigned slot, u64 cols, u64 dr, u64 dl) {
+  return ((u64)slot << kServeSlotShift) | cols | (dr << kServeFieldBits) | (dl << (2 * kServeFieldBits));
+}
+
 // ---- hash table slots --------------------------------------------------------
 //
 // A slot holds the bitwise complement of the key (so an all-zero slot is empty

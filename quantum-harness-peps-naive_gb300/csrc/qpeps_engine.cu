@@ -13,11 +13,15 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/qpeps.h"
@@ -496,7 +500,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   }
   const bool partition = p.merge == QPEPS_MERGE_PARTITION && !site;
   const size_t eb = entry_bytes(p);
-  const u32 pcap = cluster_partition_capacity();
+  const u32 pcap = partition_capacity();
   double mean = ctx.partition_fill * pcap;
   for (int attempt = 0;; ++attempt) {
     u32 parts = 0;
@@ -551,7 +555,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
                  "row expand-insert kernel");
     cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
     if (partition)
-      cuda_check(launch_partition_merge_cluster(pc, regions, cursors, view, p.n, !final_step, ctx.d_sc, ctx.stream),
+      cuda_check(launch_partition_merge(pc, regions, cursors, view, p.n, !final_step, ctx.d_sc, ctx.stream),
                  "partition merge kernel");
     else
       cuda_check(launch_compact(cfg, ctx.table.ptr, slots, view, p.n, !final_step, ctx.d_sc, ctx.stream),
@@ -1076,6 +1080,359 @@ static qpeps_options effective_options(const qpeps_options* opt) {
   return o;
 }
 
+
+// ===========================================================================
+// Serving: continuous batching of counting requests.
+//
+// A request is (N, placed prefix of k rows). Small requests share one device
+// boundary in a context of their own: keys carry the request's slot
+// (SlotLayout), every step contracts one row of every admitted request with
+// one count + scatter + merge launch triple, a request whose last row has
+// been contracted frees its slot, and queued requests are admitted between
+// steps while slots and the batch's device budget allow (an admitted
+// request's estimated peak frontier is reserved until it finishes). Requests
+// whose estimated frontier is too large for the shared batch run one at a
+// time through the row engine on a second context and stream, so their
+// kernels overlap with the batch's on the device. Repeated requests (equal N
+// and prefix, or its mirror image) can be answered from an exact result cache.
+
+using ServeClock = std::chrono::steady_clock;
+
+struct ServeRequest {
+  uint64_t tag = 0;
+  uint32_t n = 0;
+  std::vector<uint32_t> prefix;
+  ServeClock::time_point t_submit;
+  std::string cache_key;
+  double est_states = 0;
+};
+
+struct ServeSlot {
+  bool used = false;
+  uint64_t tag = 0;
+  uint32_t n = 0, k = 0;
+  unsigned rows_left = 0;
+  ServeClock::time_point t_submit, t_admit;
+  std::string cache_key;
+  double est_states = 0;
+};
+
+// Measured peak merged frontier (orbit path) per N; N=19 extrapolated.
+static double serve_peak_states(unsigned n) {
+  static const double peaks[20] = {1,        1,        2,        3,        6,         10,        21,
+                                   46,       130,      371,      4510,     22253,     98939,     541745,
+                                   2847130,  18178233, 105530452, 705792694, 4275565705.0, 2.7e10};
+  return n < 20 ? peaks[n] : 1e12;
+}
+
+// Estimated peak frontier of a request with k placed rows: each placed row
+// divides the orbit path's frontier by roughly the number of choices it made.
+static double serve_estimate(unsigned n, unsigned k) {
+  double e = serve_peak_states(n);
+  if (k >= 1) e *= 2.0 / std::max(1u, n);
+  for (unsigned i = 1; i < k; ++i) e /= std::max(1.0, (double)n - 3.0);
+  return std::max(e, 1.0);
+}
+
+static std::string serve_cache_key(unsigned n, const std::vector<uint32_t>& prefix) {
+  std::vector<uint32_t> mir(prefix.size());
+  for (size_t i = 0; i < prefix.size(); ++i) mir[i] = n - 1 - prefix[i];
+  const std::vector<uint32_t>& key = std::min(prefix, mir);  // vertical reflection preserves the count
+  std::string s = std::to_string(n) + ":";
+  for (uint32_t c : key) s += std::to_string(c) + ",";
+  return s;
+}
+
+struct Server {
+  int device = 0;
+  qpeps_serve_config cfg{};
+  Ctx* batch = nullptr;
+  Ctx* large = nullptr;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<ServeRequest> q_small, q_large;
+  std::vector<qpeps_serve_completion> done;
+  std::condition_variable cv_done;
+  bool stop = false;
+  std::thread t_batch, t_large;
+  std::map<std::string, u128> cache;
+  qpeps_serve_stats stats{};
+  std::string fatal;
+  // batch state (owned by the batch thread)
+  ServeSlot slots[kServeMaxSlots];
+  double reserved_states = 0;
+  DevBuf slot_buf;  // u64 slot_mask[64] + u64 slot_final[64][4]
+  DevFrontier f;
+};
+
+static void serve_complete(Server& sv, uint64_t tag, uint32_t n, uint32_t k, u128 count, int status, uint32_t path,
+                           ServeClock::time_point t_submit, ServeClock::time_point t_admit) {
+  const auto now = ServeClock::now();
+  qpeps_serve_completion c{};
+  c.tag = tag;
+  c.count = to_abi(count);
+  c.status = status;
+  c.n = n;
+  c.k = k;
+  c.path = path;
+  c.latency_s = std::chrono::duration<double>(now - t_submit).count();
+  c.queue_s = std::chrono::duration<double>(t_admit - t_submit).count();
+  {
+    std::lock_guard<std::mutex> lk(sv.mu);
+    sv.done.push_back(c);
+    sv.stats.completed += 1;
+  }
+  sv.cv_done.notify_all();
+}
+
+// Host-side seed boundary of a request: the prefix boundary (weight 1), or
+// for k = 0 the first-row orbit states (weights 2/1). Returns false for an
+// attacked prefix.
+static bool serve_seeds(unsigned n, const std::vector<uint32_t>& prefix, std::vector<std::pair<State, u64>>& out,
+                        unsigned* row0) {
+  const u64 mask = (1ull << n) - 1;
+  out.clear();
+  if (prefix.empty()) {
+    for (unsigned c = 0; c < n; ++c) {
+      const unsigned mirror = n - 1 - c;
+      if (c > mirror) continue;
+      const u64 b = 1ull << c;
+      State s{b, (b << 1) & mask, b >> 1};
+      out.push_back({s, c == mirror ? 1ull : 2ull});
+    }
+    *row0 = 1;
+    return true;
+  }
+  State s{0, 0, 0};
+  for (uint32_t c : prefix) {
+    const u64 b = 1ull << c;
+    if ((s.cols | s.dr | s.dl) & b) return false;
+    s = State{s.cols | b, ((s.dr | b) << 1) & mask, (s.dl | b) >> 1};
+  }
+  out.push_back({s, 1});
+  *row0 = (unsigned)prefix.size();
+  return true;
+}
+
+static void serve_batch_loop(Server& sv) {
+  Ctx& ctx = *sv.batch;
+  cuda_check(cudaSetDevice(sv.device), "cudaSetDevice");
+  Plan p{};
+  p.n = 19;
+  p.R = 2;
+  p.key_bits = 64;
+  p.grain = QPEPS_GRAIN_ROW;
+  p.merge = QPEPS_MERGE_PARTITION;
+  p.budget = (size_t)sv.cfg.batch_budget_bytes;
+  p.threads = 256;
+  p.tail_row = p.n;
+  const size_t eb = entry_bytes(p);
+  buf_reserve(ctx, sv.slot_buf, kServeMaxSlots * 5 * sizeof(u64), p.budget, "serve slots");
+  u64* d_mask = static_cast<u64*>(sv.slot_buf.ptr);
+  unsigned long long* d_final = reinterpret_cast<unsigned long long*>(d_mask + kServeMaxSlots);
+  u64 h_mask[kServeMaxSlots] = {0};
+  cuda_check(cudaMemsetAsync(sv.slot_buf.ptr, 0, kServeMaxSlots * 5 * sizeof(u64), ctx.stream), "clear slots");
+  const double budget_states = (double)p.budget / (2.4 * (double)eb);
+  std::vector<u64> seed_keys;
+  std::vector<uint32_t> seed_res;
+  std::vector<std::pair<State, u64>> seeds;
+  unsigned long long h_final[kServeMaxSlots * 4];
+  while (true) {
+    // Admission.
+    seed_keys.clear();
+    seed_res.clear();
+    bool mask_dirty = false;
+    {
+      std::unique_lock<std::mutex> lk(sv.mu);
+      bool any = false;
+      for (const ServeSlot& sl : sv.slots) any = any || sl.used;
+      if (!any && sv.q_small.empty()) {
+        if (sv.stop) break;
+        sv.cv.wait_for(lk, std::chrono::milliseconds(50));
+        continue;
+      }
+      while (!sv.q_small.empty()) {
+        ServeRequest& rq = sv.q_small.front();
+        int free_slot = -1;
+        for (unsigned i = 0; i < std::min<unsigned>(sv.cfg.max_slots, kServeMaxSlots); ++i)
+          if (!sv.slots[i].used) {
+            free_slot = (int)i;
+            break;
+          }
+        if (free_slot < 0) break;
+        if (any && sv.reserved_states + rq.est_states > budget_states) break;
+        unsigned row0 = 0;
+        ServeRequest r = std::move(rq);
+        sv.q_small.pop_front();
+        lk.unlock();
+        const auto t_admit = ServeClock::now();
+        if (!serve_seeds(r.n, r.prefix, seeds, &row0)) {
+          serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), 0, QPEPS_OK, 3, r.t_submit, t_admit);
+        } else if (row0 >= r.n) {
+          serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), 1, QPEPS_OK, 3, r.t_submit, t_admit);
+        } else {
+          ServeSlot& sl = sv.slots[free_slot];
+          sl.used = true;
+          sl.tag = r.tag;
+          sl.n = r.n;
+          sl.k = (uint32_t)r.prefix.size();
+          sl.rows_left = r.n - row0;
+          sl.t_submit = r.t_submit;
+          sl.t_admit = t_admit;
+          sl.cache_key = r.cache_key;
+          sl.est_states = r.est_states;
+          sv.reserved_states += r.est_states;
+          h_mask[free_slot] = (1ull << r.n) - 1;
+          mask_dirty = true;
+          for (auto& sd : seeds) {
+            seed_keys.push_back(serve_key((unsigned)free_slot, sd.first.cols, sd.first.dr, sd.first.dl));
+            seed_res.push_back((uint32_t)(sd.second % kPrimes[0]));
+            seed_res.push_back((uint32_t)(sd.second % kPrimes[1]));
+          }
+          any = true;
+        }
+        lk.lock();
+      }
+    }
+    if (mask_dirty)
+      cuda_check(cudaMemcpyAsync(d_mask, h_mask, sizeof h_mask, cudaMemcpyHostToDevice, ctx.stream), "slot masks");
+    if (!seed_keys.empty()) {
+      // Append the seeds to the shared boundary.
+      const u64 m = seed_keys.size();
+      if (!ensure_front(ctx, p, sv.f, sv.f.count + m, ctx.table.bytes))
+        fail(QPEPS_ERR_CAPACITY, "serving batch budget cannot hold the admitted seeds");
+      char* base = static_cast<char*>(ctx.front[0].ptr);
+      cuda_check(cudaMemcpyAsync(base + sv.f.count * 8, seed_keys.data(), m * 8, cudaMemcpyHostToDevice, ctx.stream),
+                 "seed keys");
+      std::vector<uint32_t> plane(m);
+      for (int r = 0; r < 2; ++r) {
+        for (u64 i = 0; i < m; ++i) plane[i] = seed_res[2 * i + r];
+        cuda_check(cudaMemcpyAsync(base + sv.f.cap * 8 + ((size_t)r * sv.f.cap + sv.f.count) * 4, plane.data(), m * 4,
+                                   cudaMemcpyHostToDevice, ctx.stream),
+                   "seed residues");
+        cuda_check(cudaStreamSynchronize(ctx.stream), "seed upload");
+      }
+      sv.f.count += m;
+    }
+    bool active = false;
+    for (const ServeSlot& sl : sv.slots) active = active || sl.used;
+    if (!active) continue;
+    // One row for every admitted request.
+    StepScalars* sc = ctx.d_sc;
+    cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
+    FrontierView view = view_of(p, ctx.front[0], sv.f.cap);
+    cuda_check(launch_serve_count(view, sv.f.count, d_mask, sc, ctx.sms, ctx.stream), "serve count");
+    sync_scalars(ctx);
+    const u64 terms = ctx.h_sc->terms;
+    if (terms > 0) {
+      const u32 pcap = partition_capacity();
+      double mean = ctx.partition_fill * pcap;
+      for (int attempt = 0;; ++attempt) {
+        const u32 parts = (u32)std::max<u64>(1, (u64)((double)terms / mean) + 1);
+        const size_t region_bytes = (size_t)parts * pcap * candidate_bytes(2);
+        const size_t table_bytes = region_bytes + ((size_t)parts * 4 + 255) / 256 * 256;
+        if (ctx.table.bytes < table_bytes) buf_release(ctx, ctx.table);
+        if (!ensure_front(ctx, p, sv.f, std::max<u64>(sv.f.count, terms), ctx.table.ptr ? 0 : table_bytes))
+          fail(QPEPS_ERR_CAPACITY, "serving batch budget exceeded");
+        buf_reserve(ctx, ctx.table, table_bytes, p.budget, "serve partitions");
+        view = view_of(p, ctx.front[0], sv.f.cap);
+        uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
+        PartitionCfg pc{2, ctx.sms, parts, pcap, 2};
+        cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear cursors");
+        cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
+        cuda_check(launch_serve_scatter(pc, view, sv.f.count, d_mask, ctx.table.ptr, cursors, sc, ctx.stream),
+                   "serve scatter");
+        cuda_check(launch_serve_merge(pc, ctx.table.ptr, cursors, view, d_mask, d_final, sc, ctx.stream),
+                   "serve merge");
+        sync_scalars(ctx);
+        if (ctx.h_sc->error & kErrOverflow) {
+          if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, "serving partition overflow persists");
+          mean *= 0.6;
+          continue;
+        }
+        if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, "serving device capacity error");
+        break;
+      }
+      sv.f.count = ctx.h_sc->out_count;
+    } else {
+      sv.f.count = 0;
+    }
+    {
+      std::lock_guard<std::mutex> lk(sv.mu);
+      sv.stats.batch_steps += 1;
+    }
+    // Finished requests.
+    bool any_done = false;
+    for (ServeSlot& sl : sv.slots)
+      if (sl.used && --sl.rows_left == 0) any_done = true;
+    if (!any_done) continue;
+    cuda_check(cudaMemcpyAsync(h_final, d_final, sizeof h_final, cudaMemcpyDeviceToHost, ctx.stream), "slot finals");
+    cuda_check(cudaStreamSynchronize(ctx.stream), "slot finals");
+    for (unsigned i = 0; i < kServeMaxSlots; ++i) {
+      ServeSlot& sl = sv.slots[i];
+      if (!sl.used || sl.rows_left != 0) continue;
+      u64 res[2] = {h_final[i * 4 + 0] % kPrimes[0], h_final[i * 4 + 1] % kPrimes[1]};
+      const u128 count = crt_reconstruct(res, 2);
+      cuda_check(cudaMemsetAsync(d_final + i * 4, 0, 4 * sizeof(u64), ctx.stream), "reset slot");
+      h_mask[i] = 0;
+      sl.used = false;
+      {
+        std::lock_guard<std::mutex> lk(sv.mu);
+        sv.reserved_states -= sl.est_states;
+        if (sv.cfg.use_cache) sv.cache[sl.cache_key] = count;
+      }
+      serve_complete(sv, sl.tag, sl.n, sl.k, count, QPEPS_OK, 0, sl.t_submit, sl.t_admit);
+    }
+  }
+}
+
+static void serve_large_loop(Server& sv) {
+  cuda_check(cudaSetDevice(sv.device), "cudaSetDevice");
+  while (true) {
+    ServeRequest r;
+    {
+      std::unique_lock<std::mutex> lk(sv.mu);
+      sv.cv.wait(lk, [&] { return sv.stop || !sv.q_large.empty(); });
+      if (sv.q_large.empty()) break;
+      r = std::move(sv.q_large.front());
+      sv.q_large.pop_front();
+    }
+    const auto t_admit = ServeClock::now();
+    qpeps_options o;
+    qpeps_options_default(&o);
+    o.device_budget_bytes = sv.cfg.large_budget_bytes;
+    Contraction con;
+    int status = QPEPS_OK;
+    u128 count = 0;
+    try {
+      contract(*sv.large, r.n, o, r.prefix.empty() ? nullptr : r.prefix.data(), (unsigned)r.prefix.size(), con);
+      count = con.count;
+    } catch (const Failure& e) {
+      status = e.code;
+    }
+    {
+      std::lock_guard<std::mutex> lk(sv.mu);
+      sv.stats.large_runs += 1;
+      if (status == QPEPS_OK && sv.cfg.use_cache) sv.cache[r.cache_key] = count;
+    }
+    serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), count, status, 1, r.t_submit, t_admit);
+  }
+}
+
+static void serve_thread_main(Server& sv, bool large) {
+  try {
+    if (large)
+      serve_large_loop(sv);
+    else
+      serve_batch_loop(sv);
+  } catch (const Failure& e) {
+    std::lock_guard<std::mutex> lk(sv.mu);
+    sv.fatal = e.msg;
+    sv.stop = true;
+  }
+  sv.cv.notify_all();
+  sv.cv_done.notify_all();
+}
 }  // namespace qpeps
 
 using namespace qpeps;
@@ -1154,6 +1511,123 @@ int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, 
     for (uint32_t i = 0; i < len; ++i) c.push_back(CEntryH{legs[i], values[i]});
     certify_c(c);
   });
+}
+
+void qpeps_serve_config_default(qpeps_serve_config* cfg) {
+  std::memset(cfg, 0, sizeof *cfg);
+  cfg->struct_size = sizeof(qpeps_serve_config);
+  cfg->max_slots = kServeMaxSlots;
+  cfg->use_cache = 1;
+}
+
+int qpeps_serve_open(int device, const qpeps_serve_config* cfg, void** server_out, char* err, size_t err_len) {
+  return guarded(err, err_len, [&] {
+    if (!server_out) fail(QPEPS_ERR_INVALID, "null server output");
+    Server* sv = new Server();
+    try {
+      qpeps_serve_config_default(&sv->cfg);
+      if (cfg) {
+        if (cfg->struct_size != sizeof(qpeps_serve_config)) fail(QPEPS_ERR_INVALID, "qpeps_serve_config.struct_size mismatch");
+        sv->cfg = *cfg;
+      }
+      if (sv->cfg.max_slots == 0 || sv->cfg.max_slots > kServeMaxSlots) sv->cfg.max_slots = kServeMaxSlots;
+      sv->device = device;
+      sv->batch = ctx_create(device);
+      sv->large = ctx_create(device);
+      size_t fr = 0, tot = 0;
+      cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+      if (!sv->cfg.batch_budget_bytes) sv->cfg.batch_budget_bytes = (uint64_t)(fr * 0.25);
+      if (!sv->cfg.large_budget_bytes) sv->cfg.large_budget_bytes = (uint64_t)(fr * 0.60);
+      if (!sv->cfg.large_threshold_states)
+        sv->cfg.large_threshold_states = (uint64_t)((double)sv->cfg.batch_budget_bytes / (2.4 * 16.0) / 4.0);
+      sv->t_batch = std::thread(serve_thread_main, std::ref(*sv), false);
+      sv->t_large = std::thread(serve_thread_main, std::ref(*sv), true);
+    } catch (...) {
+      if (sv->batch) ctx_free(sv->batch);
+      if (sv->large) ctx_free(sv->large);
+      delete sv;
+      throw;
+    }
+    *server_out = sv;
+  });
+}
+
+int qpeps_serve_submit(void* server, uint32_t n, const uint32_t* prefix, uint32_t k, uint64_t tag, char* err,
+                       size_t err_len) {
+  return guarded(err, err_len, [&] {
+    Server* sv = static_cast<Server*>(server);
+    if (!sv) fail(QPEPS_ERR_INVALID, "null server");
+    if (n < 1 || n > 19) fail(QPEPS_ERR_RANGE, "serving supports 1 <= N <= 19");
+    if (k > n || (k && !prefix)) fail(QPEPS_ERR_RANGE, "prefix longer than the board");
+    ServeRequest r;
+    r.tag = tag;
+    r.n = n;
+    r.prefix.assign(prefix, prefix + k);
+    for (uint32_t c : r.prefix)
+      if (c >= n) fail(QPEPS_ERR_RANGE, "prefix column out of range");
+    r.t_submit = ServeClock::now();
+    r.cache_key = serve_cache_key(n, r.prefix);
+    r.est_states = serve_estimate(n, k);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (!sv->fatal.empty()) fail(QPEPS_ERR_CUDA, "server stopped: " + sv->fatal);
+    sv->stats.submitted += 1;
+    if (sv->cfg.use_cache) {
+      auto it = sv->cache.find(r.cache_key);
+      if (it != sv->cache.end()) {
+        const u128 count = it->second;
+        sv->stats.cache_hits += 1;
+        lk.unlock();
+        serve_complete(*sv, tag, n, k, count, QPEPS_OK, 2, r.t_submit, r.t_submit);
+        return;
+      }
+    }
+    if (r.est_states > (double)sv->cfg.large_threshold_states)
+      sv->q_large.push_back(std::move(r));
+    else
+      sv->q_small.push_back(std::move(r));
+    lk.unlock();
+    sv->cv.notify_all();
+  });
+}
+
+int qpeps_serve_poll(void* server, qpeps_serve_completion* out, uint32_t cap, uint32_t* got, uint32_t wait_ms) {
+  Server* sv = static_cast<Server*>(server);
+  if (!sv || !got) return QPEPS_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(sv->mu);
+  if (sv->done.empty() && wait_ms)
+    sv->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !sv->done.empty() || !sv->fatal.empty(); });
+  const uint32_t m = (uint32_t)std::min<size_t>(cap, sv->done.size());
+  for (uint32_t i = 0; i < m; ++i) out[i] = sv->done[i];
+  sv->done.erase(sv->done.begin(), sv->done.begin() + m);
+  *got = m;
+  return sv->fatal.empty() ? QPEPS_OK : QPEPS_ERR_CUDA;
+}
+
+int qpeps_serve_stats_get(void* server, qpeps_serve_stats* out) {
+  Server* sv = static_cast<Server*>(server);
+  if (!sv || !out) return QPEPS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  *out = sv->stats;
+  return QPEPS_OK;
+}
+
+void qpeps_serve_close(void* server) {
+  Server* sv = static_cast<Server*>(server);
+  if (!sv) return;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+  }
+  sv->cv.notify_all();
+  if (sv->t_batch.joinable()) sv->t_batch.join();
+  if (sv->t_large.joinable()) sv->t_large.join();
+  cudaSetDevice(sv->device);
+  if (sv->batch) {
+    buf_release(*sv->batch, sv->slot_buf);
+    ctx_free(sv->batch);
+  }
+  if (sv->large) ctx_free(sv->large);
+  delete sv;
 }
 
 }  // extern "C"

@@ -91,12 +91,20 @@ cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, 
                                    const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
                                    cudaStream_t stream);
 
-// Merge through a 4-CTA cluster sharing a distributed shared-memory table;
-// partitions hold cluster_partition_capacity() candidates.
-uint32_t cluster_partition_capacity();
-cudaError_t launch_partition_merge_cluster(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
-                                           const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
-                                           cudaStream_t stream);
+
+
+// Serving (slotted keys, R = 2): count, scatter and merge of a boundary
+// shared by requests of different board sizes. slot_mask[s] is the board mask
+// of the request in slot s; finished boards are summed into
+// slot_final[s * 4 + r] and leave the boundary.
+cudaError_t launch_serve_count(const FrontierView& in, uint64_t n_in, const uint64_t* slot_mask, StepScalars* sc,
+                               int sms, cudaStream_t stream);
+cudaError_t launch_serve_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in,
+                                 const uint64_t* slot_mask, void* regions, uint32_t* cursors, StepScalars* sc,
+                                 cudaStream_t stream);
+cudaError_t launch_serve_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                               const FrontierView& out, const uint64_t* slot_mask, unsigned long long* slot_final,
+                               StepScalars* sc, cudaStream_t stream);
 
 // Slice-tail kernel control block (device memory). Row statistics per tail
 // row q (row0 + q): [0] input states, [1] output states, [2] successor terms,

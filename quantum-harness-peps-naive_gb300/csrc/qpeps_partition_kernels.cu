@@ -13,7 +13,6 @@
 // This replaces the reference's `candidates.sort_unstable_by_key` + checked
 // reduce (src/lib.rs:5353-5367): equal packed keys are merged by addition;
 // the order of the output boundary is not observable by any metric.
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "qpeps_device.cuh"
@@ -25,7 +24,7 @@ namespace {
 
 constexpr u32 kFullMask = 0xffffffffu;
 
-__device__ __forceinline__ u64 pboard_mask(unsigned n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
+__host__ __device__ __forceinline__ u64 pboard_mask_host(unsigned n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
 
 __device__ __forceinline__ int pwarp_inclusive_scan(int v) {
   const int lane = threadIdx.x & 31;
@@ -110,10 +109,10 @@ __device__ __forceinline__ unsigned long long pblock_sum(unsigned long long v) {
 constexpr int kPPL = 2;  // parents per lane per iteration
 constexpr int kKB = 4;   // successor rounds per atomic batch
 
-template <int R, int BLOCK>
+template <int R, int BLOCK, typename Layout>
 __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __restrict__ keys,
                                                                   const u32* __restrict__ res, u64 res_stride,
-                                                                  u64 n_in, unsigned n, Cand<R>* __restrict__ regions,
+                                                                  u64 n_in, Layout L, Cand<R>* __restrict__ regions,
                                                                   u32* __restrict__ cursors, u32 parts, u32 cap,
                                                                   StepScalars* __restrict__ sc) {
   constexpr int WARPS = BLOCK / 32;
@@ -122,7 +121,6 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
   __shared__ u64 s_free[WARPS][PW];
   __shared__ u32 s_w[WARPS][R][PW];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const u64 mask = pboard_mask(n);
   const u64 gwarp = (u64)blockIdx.x * WARPS + wid;
   const u64 stride = (u64)gridDim.x * WARPS * PW;
   bool overflow = false;
@@ -151,8 +149,8 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
     for (int q = 0; q < kPPL; ++q) {
       u64 fr = 0;
       if (nkey[q] != kEmptyKey) {
-        const State s = unpack<u64>(nkey[q], n, mask);
-        fr = ~(s.cols | s.dr | s.dl) & mask;
+        const State s = L.unpack(nkey[q]);
+        fr = ~(s.cols | s.dr | s.dl) & L.mask_of(nkey[q]);
       }
       s_key[wid][q * 32 + lane] = nkey[q];
       s_free[wid][q * 32 + lane] = fr;
@@ -187,9 +185,10 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
           const int q = t < oc0 ? 0 : 1;
           if (q) t -= oc0;
           const int slot = q * 32 + owner;
-          const State s = unpack<u64>(s_key[wid][slot], n, mask);
+          const u64 pkey = s_key[wid][slot];
+          const State s = L.unpack(pkey);
           const unsigned col = pnth_set_bit(s_free[wid][slot], t);
-          c[k].key = row_successor<u64>(s, 1ull << col, n, mask);
+          c[k].key = L.successor(pkey, s, 1ull << col);
 #pragma unroll
           for (int r = 0; r < R; ++r) c[k].res[r] = s_w[wid][r][slot];
           part[k] = partition_of(mix64(c[k].key), parts);
@@ -221,11 +220,11 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
 
 constexpr u64 kEmpty = kEmptyKey;
 
-template <int R, int BLOCK, int H, int CAP>
+template <int R, int BLOCK, int H, int CAP, typename Layout>
 __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* __restrict__ regions,
                                                                 const u32* __restrict__ cursors, u32 parts,
                                                                 u64* __restrict__ keys_out, u32* __restrict__ res_out,
-                                                                u64 out_stride, unsigned n, int write_out,
+                                                                u64 out_stride, Layout L, int write_out,
                                                                 StepScalars* __restrict__ sc) {
   constexpr int WARPS = BLOCK / 32;
   constexpr int PER = H / BLOCK;    // table slots per thread
@@ -236,8 +235,11 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [R][H]
   __shared__ u32 s_cnt[PER * WARPS];
   __shared__ unsigned long long s_base;
+  // Serving: finished boards are summed per request slot here, then flushed.
+  __shared__ unsigned long long s_slot_fin[Layout::kSlotted ? kServeMaxSlots * R : 1];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const u64 mask = pboard_mask(n);
+  if constexpr (Layout::kSlotted)
+    for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK) s_slot_fin[i] = 0ull;
   // A partition overflowed in the scatter: write nothing, so the boundary
   // buffer (read by the scatter, written here in place) stays intact for the
   // host's retry with smaller partitions.
@@ -298,7 +300,21 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
     u32 flags = 0;
 #pragma unroll
     for (int it = 0; it < PER; ++it) {
-      const bool occ = s_key[it * BLOCK + threadIdx.x] != kEmpty;
+      bool occ = s_key[it * BLOCK + threadIdx.x] != kEmpty;
+      if constexpr (Layout::kSlotted) {
+        // A finished board leaves the boundary: sum it into its slot.
+        const u64 key = s_key[it * BLOCK + threadIdx.x];
+        if (occ && (key & L.mask_of(key)) == L.mask_of(key)) {
+          const int slot = it * BLOCK + threadIdx.x;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            atomicAdd(&s_slot_fin[L.slot(key) * R + r], s_acc[r * H + slot] % prime_at(r));
+            s_acc[r * H + slot] = 0ull;
+          }
+          s_key[slot] = kEmpty;
+          occ = false;
+        }
+      }
       flags |= (u32)occ << it;
       const u32 b = __ballot_sync(kFullMask, occ);
       if (lane == 0) s_cnt[it * WARPS + wid] = __popc(b);
@@ -333,7 +349,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
         const int slot = it * BLOCK + threadIdx.x;
         const u64 key = s_key[slot];
         const u64 idx = base + s_cnt[it * WARPS + wid] + __popc(b & ((1u << lane) - 1u));
-        const bool full = (key & mask) == mask;
+        const bool full = (key & L.mask_of(key)) == L.mask_of(key);
         if (write_out) keys_out[idx] = key;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -358,166 +374,26 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   }
   const unsigned long long t = pblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+  if constexpr (Layout::kSlotted) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK)
+      if (s_slot_fin[i]) atomicAdd(&L.slot_final[(i / R) * 4 + (i % R)], s_slot_fin[i]);
+  }
 }
 
-// ---------------------------------------------------------------------------
-// Cluster merge. A thread-block cluster of CL CTAs shares one distributed
-// shared-memory table of CL*H slots (each CTA owns H), so one partition can
-// hold CL*H/2 candidates. Bigger partitions mean fewer open partition tails
-// for the scatter (they must stay in L2 for its 16-byte stores to be
-// write-combined). Each CTA loads a quarter of the partition, inserts every
-// candidate into its home CTA's table with DSMEM atomics (home and slot come
-// from the low hash bits, independent of the high bits that chose the
-// partition), and after a cluster barrier compacts and resets its own table.
-
-template <int R, int BLOCK, int H, int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BLOCK)
-    partition_merge_cluster_kernel(const Cand<R>* __restrict__ regions, const u32* __restrict__ cursors, u32 parts,
-                                   u64* __restrict__ keys_out, u32* __restrict__ res_out, u64 out_stride, unsigned n,
-                                   int write_out, StepScalars* __restrict__ sc) {
-  namespace cg = cooperative_groups;
-  constexpr int WARPS = BLOCK / 32;
-  constexpr int PER = H / BLOCK;
-  constexpr int CAP = CL * H / 2;
-  constexpr int SLICE = CAP / CL;
-  constexpr int LPT = SLICE / BLOCK;
-  static_assert(H % BLOCK == 0 && SLICE % BLOCK == 0 && PER <= 32 && (PER * WARPS) % 32 == 0, "shape");
-  static_assert((CL & (CL - 1)) == 0 && (H & (H - 1)) == 0, "power-of-two cluster and table");
-  cg::cluster_group cluster = cg::this_cluster();
-  const unsigned rank = cluster.block_rank();
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  u64* s_key = reinterpret_cast<u64*>(smem_raw);
-  unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [R][H]
-  __shared__ u32 s_cnt[PER * WARPS];
-  __shared__ unsigned long long s_base;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const u64 mask = pboard_mask(n);
-  if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;  // uniform across the cluster
-  unsigned long long wsum[R], fsum[R], fstates = 0;
-#pragma unroll
-  for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
-  for (int i = threadIdx.x; i < H; i += BLOCK) {
-    s_key[i] = kEmpty;
-#pragma unroll
-    for (int r = 0; r < R; ++r) s_acc[r * H + i] = 0ull;
+// Successor count of a slotted (serving) boundary.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) slot_count_kernel(const u64* __restrict__ keys, u64 n_in, SlotLayout L,
+                                                           StepScalars* __restrict__ sc) {
+  unsigned long long acc = 0;
+  for (u64 i = (u64)blockIdx.x * BLOCK + threadIdx.x; i < n_in; i += (u64)gridDim.x * BLOCK) {
+    const u64 key = keys[i];
+    const State s = L.unpack(key);
+    acc += __popcll(~(s.cols | s.dr | s.dl) & L.mask_of(key));
   }
-  u64* rkey[CL];
-  unsigned long long* racc[CL];
-#pragma unroll
-  for (int c = 0; c < CL; ++c) {
-    rkey[c] = cluster.map_shared_rank(s_key, c);
-    racc[c] = cluster.map_shared_rank(s_acc, c);
-  }
-  const u32 cid = blockIdx.x / CL, ncl = gridDim.x / CL;
-  Cand<R> buf[LPT];
-  u32 bcnt = 0;
-  auto fetch = [&](u32 part) {
-    bcnt = min(cursors[part], (u32)CAP);
-    const Cand<R>* src = regions + (u64)part * CAP;
-#pragma unroll
-    for (int l = 0; l < LPT; ++l) {
-      const u32 i = rank * SLICE + l * BLOCK + threadIdx.x;
-      if (i < bcnt) buf[l] = load_cand<R>(src + i);
-    }
-  };
-  u32 part = cid;
-  if (part < parts) fetch(part);
-  cluster.sync();
-  for (; part < parts; part += ncl) {
-#pragma unroll
-    for (int l = 0; l < LPT; ++l) {
-      const u32 i = rank * SLICE + l * BLOCK + threadIdx.x;
-      if (i < bcnt) {
-        const Cand<R>& c = buf[l];
-        const u64 h = mix64(c.key);
-        const int home = (int)(h & (CL - 1));
-        u64* tk = rkey[home];
-        unsigned long long* ta = racc[home];
-        u32 slot = (u32)(h >> 8) & (H - 1);
-        for (int probe = 0; probe < H; ++probe) {
-          u64 cur = tk[slot];
-          if (cur == kEmpty) {
-            cur = atomicCAS(reinterpret_cast<unsigned long long*>(&tk[slot]), kEmpty, c.key);
-            if (cur == kEmpty) cur = c.key;
-          }
-          if (cur == c.key) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) atomicAdd(&ta[r * H + slot], (unsigned long long)c.res[r]);
-            break;
-          }
-          slot = (slot + 1) & (H - 1);
-        }
-      }
-    }
-    cluster.sync();
-    const u32 next = part + ncl;
-    if (next < parts) fetch(next);
-    u32 flags = 0;
-#pragma unroll
-    for (int it = 0; it < PER; ++it) {
-      const bool occ = s_key[it * BLOCK + threadIdx.x] != kEmpty;
-      flags |= (u32)occ << it;
-      const u32 b = __ballot_sync(kFullMask, occ);
-      if (lane == 0) s_cnt[it * WARPS + wid] = __popc(b);
-    }
-    __syncthreads();
-    if (wid == 0) {
-      constexpr int PL = PER * WARPS / 32;
-      u32 v[PL];
-      u32 sum = 0;
-#pragma unroll
-      for (int q = 0; q < PL; ++q) {
-        v[q] = s_cnt[lane * PL + q];
-        sum += v[q];
-      }
-      const int incl = pwarp_inclusive_scan((int)sum);
-      u32 run = (u32)incl - sum;
-#pragma unroll
-      for (int q = 0; q < PL; ++q) {
-        s_cnt[lane * PL + q] = run;
-        run += v[q];
-      }
-      const int tot = __shfl_sync(kFullMask, incl, 31);
-      if (lane == 0) s_base = tot ? atomicAdd(&sc->out_count, (unsigned long long)tot) : 0ull;
-    }
-    __syncthreads();
-    const unsigned long long base = s_base;
-#pragma unroll
-    for (int it = 0; it < PER; ++it) {
-      const bool occ = (flags >> it) & 1u;
-      const u32 b = __ballot_sync(kFullMask, occ);
-      if (occ) {
-        const int slot = it * BLOCK + threadIdx.x;
-        const u64 key = s_key[slot];
-        const u64 idx = base + s_cnt[it * WARPS + wid] + __popc(b & ((1u << lane) - 1u));
-        const bool full = (key & mask) == mask;
-        if (write_out) keys_out[idx] = key;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const u32 v = (u32)(s_acc[r * H + slot] % prime_at(r));
-          if (write_out) res_out[r * out_stride + idx] = v;
-          wsum[r] += v;
-          if (full) fsum[r] += v;
-          s_acc[r * H + slot] = 0ull;
-        }
-        s_key[slot] = kEmpty;
-        fstates += full;
-      }
-    }
-    cluster.sync();  // tables reset before the cluster inserts the next partition
-  }
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    unsigned long long t = pblock_sum<BLOCK>(wsum[r]);
-    if (threadIdx.x == 0 && t) atomicAdd(&sc->weight_sum[r], t);
-    t = pblock_sum<BLOCK>(fsum[r]);
-    if (threadIdx.x == 0 && t) atomicAdd(&sc->final_sum[r], t);
-  }
-  const unsigned long long t = pblock_sum<BLOCK>(fstates);
-  if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+  const unsigned long long t = pblock_sum<BLOCK>(acc);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->terms, t);
 }
-
-constexpr int kClusterCTAs = 4;
 
 constexpr int kScatterBlock = 256;
 constexpr int kMergeBlock = 512;
@@ -529,77 +405,71 @@ constexpr size_t merge_smem() {
   return (size_t)kMergeH * (8 + 8 * R);
 }
 
-template <int R>
-cudaError_t scatter_impl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, unsigned n, void* regions,
+template <int R, typename Layout>
+cudaError_t scatter_impl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
                          u32* cursors, StepScalars* sc, cudaStream_t stream) {
   u64 want = (n_in + kScatterBlock * kPPL - 1) / (kScatterBlock * kPPL);
   const u64 capb = (u64)pc.sms * 8;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
-  partition_scatter_kernel<R, kScatterBlock><<<grid, kScatterBlock, 0, stream>>>(
-      reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, n, reinterpret_cast<Cand<R>*>(regions), cursors,
+  partition_scatter_kernel<R, kScatterBlock, Layout><<<grid, kScatterBlock, 0, stream>>>(
+      reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
       pc.parts, pc.cap, sc);
   return cudaGetLastError();
 }
 
-template <int R>
+template <int R, typename Layout>
 cudaError_t merge_impl(const PartitionCfg& pc, const void* regions, const u32* cursors, const FrontierView& out,
-                       unsigned n, bool write_out, StepScalars* sc, cudaStream_t stream) {
-  auto kern = partition_merge_kernel<R, kMergeBlock, kMergeH, kMergeCap>;
+                       Layout L, bool write_out, StepScalars* sc, cudaStream_t stream) {
+  auto kern = partition_merge_kernel<R, kMergeBlock, kMergeH, kMergeCap, Layout>;
   const size_t smem = merge_smem<R>();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const u64 capb = (u64)pc.sms * pc.merge_blocks_per_sm;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, capb));
   kern<<<grid, kMergeBlock, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors, pc.parts,
-                                            reinterpret_cast<u64*>(out.keys), out.res, out.cap, n, write_out ? 1 : 0,
+                                            reinterpret_cast<u64*>(out.keys), out.res, out.cap, L, write_out ? 1 : 0,
                                             sc);
-  return cudaGetLastError();
-}
-
-template <int R>
-cudaError_t merge_cluster_impl(const PartitionCfg& pc, const void* regions, const u32* cursors,
-                               const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
-                               cudaStream_t stream) {
-  auto kern = partition_merge_cluster_kernel<R, kMergeBlock, kMergeH, kClusterCTAs>;
-  const size_t smem = merge_smem<R>();
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const u64 clusters_cap = std::max<u64>(1, (u64)pc.sms * pc.merge_blocks_per_sm / kClusterCTAs);
-  const u64 clusters = std::max<u64>(1, std::min<u64>(pc.parts, clusters_cap));
-  kern<<<(unsigned)(clusters * kClusterCTAs), kMergeBlock, smem, stream>>>(
-      reinterpret_cast<const Cand<R>*>(regions), cursors, pc.parts, reinterpret_cast<u64*>(out.keys), out.res,
-      out.cap, n, write_out ? 1 : 0, sc);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-uint32_t cluster_partition_capacity() { return kClusterCTAs * kMergeH / 2; }
+size_t candidate_bytes(int residues) { return residues <= 2 ? 16 : 32; }
 
-cudaError_t launch_partition_merge_cluster(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
-                                           const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
-                                           cudaStream_t stream) {
-  if (pc.cap != cluster_partition_capacity()) return cudaErrorInvalidValue;
-  switch (pc.residues) {
-    case 1: return merge_cluster_impl<1>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 2: return merge_cluster_impl<2>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 3: return merge_cluster_impl<3>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 4: return merge_cluster_impl<4>(pc, regions, cursors, out, n, write_out, sc, stream);
-  }
-  return cudaErrorInvalidValue;
+cudaError_t launch_serve_count(const FrontierView& in, uint64_t n_in, const uint64_t* slot_mask, StepScalars* sc,
+                               int sms, cudaStream_t stream) {
+  if (n_in == 0) return cudaSuccess;
+  const u64 want = (n_in + 1023) / 1024;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(want, (u64)sms * 8));
+  slot_count_kernel<256><<<grid, 256, 0, stream>>>(reinterpret_cast<const u64*>(in.keys), n_in,
+                                                   SlotLayout{slot_mask, nullptr}, sc);
+  return cudaGetLastError();
 }
 
-size_t candidate_bytes(int residues) { return residues <= 2 ? 16 : 32; }
+cudaError_t launch_serve_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in,
+                                 const uint64_t* slot_mask, void* regions, uint32_t* cursors, StepScalars* sc,
+                                 cudaStream_t stream) {
+  if (n_in == 0) return cudaSuccess;
+  if (pc.residues != 2) return cudaErrorInvalidValue;
+  return scatter_impl<2>(pc, in, n_in, SlotLayout{slot_mask, nullptr}, regions, cursors, sc, stream);
+}
+
+cudaError_t launch_serve_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                               const FrontierView& out, const uint64_t* slot_mask, unsigned long long* slot_final,
+                               StepScalars* sc, cudaStream_t stream) {
+  if (pc.residues != 2) return cudaErrorInvalidValue;
+  return merge_impl<2>(pc, regions, cursors, out, SlotLayout{slot_mask, slot_final}, true, sc, stream);
+}
 uint32_t partition_capacity() { return kMergeCap; }
 
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
   switch (pc.residues) {
-    case 1: return scatter_impl<1>(pc, in, n_in, n, regions, cursors, sc, stream);
-    case 2: return scatter_impl<2>(pc, in, n_in, n, regions, cursors, sc, stream);
-    case 3: return scatter_impl<3>(pc, in, n_in, n, regions, cursors, sc, stream);
-    case 4: return scatter_impl<4>(pc, in, n_in, n, regions, cursors, sc, stream);
+    case 1: return scatter_impl<1>(pc, in, n_in, FixedLayout{n, pboard_mask_host(n)}, regions, cursors, sc, stream);
+    case 2: return scatter_impl<2>(pc, in, n_in, FixedLayout{n, pboard_mask_host(n)}, regions, cursors, sc, stream);
+    case 3: return scatter_impl<3>(pc, in, n_in, FixedLayout{n, pboard_mask_host(n)}, regions, cursors, sc, stream);
+    case 4: return scatter_impl<4>(pc, in, n_in, FixedLayout{n, pboard_mask_host(n)}, regions, cursors, sc, stream);
   }
   return cudaErrorInvalidValue;
 }
@@ -608,10 +478,10 @@ cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, 
                                    const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
                                    cudaStream_t stream) {
   switch (pc.residues) {
-    case 1: return merge_impl<1>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 2: return merge_impl<2>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 3: return merge_impl<3>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 4: return merge_impl<4>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 1: return merge_impl<1>(pc, regions, cursors, out, FixedLayout{n, pboard_mask_host(n)}, write_out, sc, stream);
+    case 2: return merge_impl<2>(pc, regions, cursors, out, FixedLayout{n, pboard_mask_host(n)}, write_out, sc, stream);
+    case 3: return merge_impl<3>(pc, regions, cursors, out, FixedLayout{n, pboard_mask_host(n)}, write_out, sc, stream);
+    case 4: return merge_impl<4>(pc, regions, cursors, out, FixedLayout{n, pboard_mask_host(n)}, write_out, sc, stream);
   }
   return cudaErrorInvalidValue;
 }
