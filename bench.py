@@ -294,6 +294,92 @@ def run_ours(args):
     ctx.close()
 
 
+def run_serve(args):
+    """Seeded Poisson stream of counting requests through the continuous-batching
+    server. Prints one JSON line: p50/p99 latency and requests/s."""
+    import random  # noqa: PLC0415
+
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = importlib.import_module(PACKAGE)
+    if not pkg.LIBRARY_PATH.exists():
+        pkg.build()
+    rng = random.Random(args.serve_seed)
+    reqs = []
+    t = 0.0
+    for tag in range(args.serve_requests):
+        t += rng.expovariate(args.serve_rate)
+        n = rng.randint(args.serve_nmin, args.serve_nmax)
+        k = rng.randint(0, 3)
+        reqs.append((t, tag, n, pkg.random_prefix(rng, n, k)))
+    got = {}
+    sv = pkg.Server(0, use_cache=int(not args.serve_no_cache))
+    sampler = ClockSampler(0)
+    sampler.start()
+    t0 = time.perf_counter()
+    for at, tag, n, prefix in reqs:
+        while True:
+            now = time.perf_counter() - t0
+            if now >= at:
+                break
+            for c in sv.poll(wait_ms=max(0, min(5, int((at - now) * 1e3)))):
+                got[c["tag"]] = c
+        sv.submit(n, prefix, tag)
+    deadline = time.perf_counter() + args.serve_timeout
+    while len(got) < len(reqs) and time.perf_counter() < deadline:
+        for c in sv.poll(wait_ms=50):
+            got[c["tag"]] = c
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    stats = sv.stats()
+    sv.close()
+    lat = sorted(c["latency_s"] for c in got.values())
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None  # noqa: E731
+    # Exactness: k = 0 against the known counts, small boards against the CPU oracle.
+    import oracle_py  # noqa: PLC0415
+
+    oracle_py.build()
+    checked = wrong = 0
+    for _, tag, n, prefix in reqs:
+        c = got.get(tag)
+        if c is None:
+            continue
+        if not prefix:
+            want = pkg.known_count(n)
+        elif n <= args.serve_check_nmax:
+            want = oracle_py.contract(n, symmetry=False, prefix=prefix)["count"]
+        else:
+            continue
+        checked += 1
+        wrong += int(c["count"] != want or c["status"] != 0)
+    paths = {}
+    for c in got.values():
+        paths[c["path"]] = paths.get(c["path"], 0) + 1
+    line = {
+        "metric": "serve p50/p99 latency (mixed-N prefix counting stream)",
+        "value": len(got) / wall,
+        "unit": "requests/s",
+        "n_gpus": 1,
+        "higher_is_better": True,
+        "p50_latency_s": q(0.50),
+        "p99_latency_s": q(0.99),
+        "completed": len(got),
+        "submitted": len(reqs),
+        "wall_s": wall,
+        "checked": checked,
+        "wrong": wrong,
+        "paths": paths,
+        "server": stats,
+        "clocks": clocks,
+        "config": {"workload": "Poisson stream, N ~ U{%d..%d}, k ~ U{0..3} random legal prefixes"
+                   % (args.serve_nmin, args.serve_nmax), "requests": args.serve_requests,
+                   "rate_per_s": args.serve_rate, "seed": args.serve_seed, "cache": not args.serve_no_cache},
+        "data": "synthetic (seeded request stream)",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -307,8 +393,19 @@ def main():
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve", action="store_true", help="run the serving stream instead of the Q(N) step")
+    ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
+    ap.add_argument("--serve-seed", type=int, default=20261203)
+    ap.add_argument("--serve-nmin", type=int, default=10)
+    ap.add_argument("--serve-nmax", type=int, default=19)
+    ap.add_argument("--serve-no-cache", action="store_true")
+    ap.add_argument("--serve-check-nmax", type=int, default=12)
+    ap.add_argument("--serve-timeout", type=float, default=900.0)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.serve:
+        run_serve(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -913,6 +913,27 @@ static void contract_items(Ctx& ctx, Contraction& out, const std::vector<Item>& 
   run_chunks(ctx, p, std::move(pending), out.rows, out.rs);
 }
 
+// Measured peak merged frontier (orbit path) per N (N=19: measured with
+// slicing; N >= 20: extrapolated by the x6.3 per-N growth of N=13..19).
+static double serve_peak_states(unsigned n) {
+  static const double peaks[20] = {1,        1,        2,        3,        6,         10,        21,
+                                   46,       130,      371,      4510,     22253,     98939,     541745,
+                                   2847130,  18178233, 105530452, 705792694, 4275565705.0, 2.7e10};
+  if (n < 20) return peaks[n];
+  double e = peaks[19];
+  for (unsigned i = 19; i < n; ++i) e *= 6.3;
+  return e;
+}
+
+// Estimated peak frontier of a request with k placed rows: each placed row
+// divides the orbit path's frontier by roughly the number of choices it made.
+static double serve_estimate(unsigned n, unsigned k) {
+  double e = serve_peak_states(n);
+  if (k >= 1) e *= 2.0 / std::max(1u, n);
+  for (unsigned i = 1; i < k; ++i) e /= std::max(1.0, (double)n - 3.0);
+  return std::max(e, 1.0);
+}
+
 static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
                      Contraction& out) {
   auto t0 = std::chrono::steady_clock::now();
@@ -968,8 +989,38 @@ static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_
     out.peak_states = std::max<u64>(out.peak_states, items.size());
     ++row0;
   }
-  out.slice_depth = row0;
-  contract_items(ctx, out, items, row0);
+  // Predictive slicing: when the merged frontier is estimated not to fit the
+  // device budget, contract groups of slices (first-row orbit slices, or
+  // deeper prefix slices) one chunk at a time instead of halving a live
+  // frontier at its peak and spilling it to the host.
+  if (o.slice_depth == 0 && out.plan.grain == QPEPS_GRAIN_ROW && row0 < n && !items.empty()) {
+    const double per_state = 2.0 * (double)entry_bytes(out.plan) + 1.25 * (double)candidate_bytes(out.plan.R);
+    const double cap_states = 0.8 * (double)out.plan.budget / per_state;
+    double est_total = serve_estimate(n, k);
+    while (est_total > cap_states && row0 + 2 < n) {
+      const double est_item = est_total / (double)items.size() * 1.5;
+      if (est_item <= cap_states) {
+        const size_t per_chunk = std::max<size_t>(1, (size_t)(cap_states / est_item));
+        std::vector<HostChunk> chunks;
+        for (size_t lo = 0; lo < items.size(); lo += per_chunk) {
+          std::vector<Item> part(items.begin() + lo, items.begin() + std::min(items.size(), lo + per_chunk));
+          chunks.push_back(chunk_from_items(out.plan, part, row0));
+        }
+        out.slice_depth = row0;
+        run_chunks(ctx, out.plan, std::move(chunks), out.rows, out.rs);
+        items.clear();
+        break;
+      }
+      RowAcc& acc = out.rows[row0];
+      items = host_expand(n, items, row0, false, acc);
+      acc.device_row = false;
+      ++row0;
+    }
+  }
+  if (!items.empty()) {
+    out.slice_depth = std::max(out.slice_depth, row0);
+    contract_items(ctx, out, items, row0);
+  }
   out.peak_states = std::max<u64>(out.peak_states, out.rs.peak_states);
   // Count: host-finished boards plus device final sums, then CRT.
   u64 res[kMaxResidues];
@@ -1116,23 +1167,6 @@ struct ServeSlot {
   std::string cache_key;
   double est_states = 0;
 };
-
-// Measured peak merged frontier (orbit path) per N; N=19 extrapolated.
-static double serve_peak_states(unsigned n) {
-  static const double peaks[20] = {1,        1,        2,        3,        6,         10,        21,
-                                   46,       130,      371,      4510,     22253,     98939,     541745,
-                                   2847130,  18178233, 105530452, 705792694, 4275565705.0, 2.7e10};
-  return n < 20 ? peaks[n] : 1e12;
-}
-
-// Estimated peak frontier of a request with k placed rows: each placed row
-// divides the orbit path's frontier by roughly the number of choices it made.
-static double serve_estimate(unsigned n, unsigned k) {
-  double e = serve_peak_states(n);
-  if (k >= 1) e *= 2.0 / std::max(1u, n);
-  for (unsigned i = 1; i < k; ++i) e /= std::max(1.0, (double)n - 3.0);
-  return std::max(e, 1.0);
-}
 
 static std::string serve_cache_key(unsigned n, const std::vector<uint32_t>& prefix) {
   std::vector<uint32_t> mir(prefix.size());
