@@ -5,9 +5,13 @@
 One step = one complete exact contraction of Q(N) (all rows, all first-row
 orbit slices) through the library's C ABI. Prints one JSON line.
 
-value  : boundary entries per second = (sum over row steps of boundary
-         entries read by the merge) / (device time of the whole contraction,
-         CUDA events on the library's stream).
+value  : boundary entries per second = (boundary entries of the merged
+         contraction: the sum over rows of the merged frontier's input states)
+         / (device time of the whole contraction, CUDA events on the
+         library's stream). When the library slices the frontier into device
+         batches it processes more entries than that (lost merges); those
+         are reported as boundary_entries_processed_per_step and do not
+         inflate `value`.
 e2e    : the same entries / wall time of the C-ABI call (host seeding,
          host->device upload of the seed boundary, all row steps, device->host
          read-back of every row's metrics and of the count residues).
@@ -38,6 +42,13 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 
 PACKAGE = "quantum-harness-peps-naive_gb300"
+
+# Boundary entries of the merged contraction of Q(N): the sum over rows of the
+# merged frontier's input states (the reference's LayerMetric.input_states),
+# i.e. the work unit of "boundary entries/s", independent of how a run slices
+# the frontier. N <= 16 match the CPU oracle; 17 and 18 were measured by this
+# library in single-batch merged runs (tail_row off, one device batch).
+MERGED_ENTRIES = {16: 397600651, 17: 2684482260, 18: 16682949222}
 METRIC = "Q(N) wall time & boundary entries/s at N=18 (bit-exact)"
 UNIT = "boundary entries/s"
 
@@ -212,7 +223,8 @@ def run_ours(args):
     barrier()
     clocks = sampler.stop()
 
-    entries = results[-1].device["entries_in"]
+    entries_run = results[-1].device["entries_in"]
+    entries = MERGED_ENTRIES.get(args.n, entries_run) if results[-1].device["batches"] > 1 else entries_run
     dev_s = max(sum(x.device["device_ms"] for x in results) / len(results) / 1e3, 1e-12)
     wall_s = max(t_all / args.steps, 1e-12)
     if world > 1:
@@ -275,6 +287,7 @@ def run_ours(args):
         "wall_s_per_step": wall_s,
         "device_s_per_step": dev_s,
         "boundary_entries_per_step": entries,
+        "boundary_entries_processed_per_step": entries_run,
         "peak_states": results[-1].peak_states,
         "peak_device_bytes": d["peak_device_bytes"],
         "gpu_launches": sum(x.device["gpu_launches"] for x in results),

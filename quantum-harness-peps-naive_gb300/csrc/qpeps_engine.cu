@@ -998,7 +998,8 @@ static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_
     const double cap_states = 0.8 * (double)out.plan.budget / per_state;
     double est_total = serve_estimate(n, k);
     while (est_total > cap_states && row0 + 2 < n) {
-      const double est_item = est_total / (double)items.size() * 1.5;
+      // Slices are uneven (centre columns carry more states): margin 2.
+      const double est_item = est_total / (double)items.size() * 2.0;
       if (est_item <= cap_states) {
         const size_t per_chunk = std::max<size_t>(1, (size_t)(cap_states / est_item));
         std::vector<HostChunk> chunks;
