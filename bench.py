@@ -293,7 +293,8 @@ def run_ours(args):
         "gpu_launches": sum(x.device["gpu_launches"] for x in results),
         "clocks": clocks,
         "roofline": roofline,
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": d["h2d_bytes"],
+                "d2h_bytes_per_step": d["d2h_bytes"]},
     }
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -404,7 +405,7 @@ def main():
     ap.add_argument("--slice-depth", type=int, default=0)
     ap.add_argument("--tail-row", type=int, default=None,
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
-    ap.add_argument("--cpu-rows", type=int, default=8)
+    ap.add_argument("--cpu-rows", type=int, default=9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve", action="store_true", help="run the serving stream instead of the Q(N) step")
     ap.add_argument("--serve-requests", type=int, default=10000)

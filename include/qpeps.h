@@ -95,6 +95,8 @@ typedef struct qpeps_result {
   uint64_t tail_items;        /* boundary entries handed to the slice-tail kernel */
   uint64_t tail_overflow;     /* of those, entries redone by the row engine */
   double tail_kernel_ms;      /* device time of the slice-tail kernel */
+  uint64_t h2d_bytes;         /* host->device bytes copied by this call */
+  uint64_t d2h_bytes;         /* device->host bytes copied by this call */
   uint32_t residue_primes[4];
   uint64_t count_residues[4];
 } qpeps_result;

@@ -98,6 +98,8 @@ class Result(ctypes.Structure):
         ("tail_items", ctypes.c_uint64),
         ("tail_overflow", ctypes.c_uint64),
         ("tail_kernel_ms", ctypes.c_double),
+        ("h2d_bytes", ctypes.c_uint64),
+        ("d2h_bytes", ctypes.c_uint64),
         ("residue_primes", ctypes.c_uint32 * 4),
         ("count_residues", ctypes.c_uint64 * 4),
     ]
@@ -321,6 +323,8 @@ def _result_from(res: Result, layers: Sequence[Layer] | None) -> ContractionResu
         "tail_items": res.tail_items,
         "tail_overflow": res.tail_overflow,
         "tail_kernel_ms": res.tail_kernel_ms,
+        "h2d_bytes": res.h2d_bytes,
+        "d2h_bytes": res.d2h_bytes,
         "residue_primes": list(res.residue_primes)[: res.residues],
         "count_residues": list(res.count_residues)[: res.residues],
     }

@@ -273,6 +273,7 @@ struct Ctx {
   CTableDev c_dev;
   bool c_uploaded = false;
   double partition_fill = 0.83;  // target candidates per partition / partition slots
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued (since context creation)
   DevBuf tail;                   // TailControl + overflow list
 };
 
@@ -401,6 +402,7 @@ static u64 pow2_at_least(u64 x) {
 static void sync_scalars(Ctx& ctx) {
   cuda_check(cudaMemcpyAsync(ctx.h_sc, ctx.d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, ctx.stream),
              "read step scalars");
+  ctx.d2h_bytes += sizeof(StepScalars);
   cuda_check(cudaStreamSynchronize(ctx.stream), "step synchronize");
 }
 
@@ -617,6 +619,7 @@ static void split_to_host(Ctx& ctx, const Plan& p, DevFrontier& f, unsigned row,
                                moved * 4, cudaMemcpyDeviceToHost, ctx.stream),
                "spill residues");
   cuda_check(cudaStreamSynchronize(ctx.stream), "spill synchronize");
+  ctx.d2h_bytes += moved * (kb + 4u * p.R);
   f.count = keep;
   pending.push_back(std::move(hc));
 }
@@ -640,6 +643,7 @@ static void upload_chunk(Ctx& ctx, const Plan& p, const HostChunk& hc, DevFronti
                                hc.count * 4, cudaMemcpyHostToDevice, ctx.stream),
                "upload residues");
   cuda_check(cudaStreamSynchronize(ctx.stream), "upload synchronize");
+  ctx.h2d_bytes += hc.count * (kb + 4u * p.R);
   f.count = hc.count;
 }
 
@@ -845,6 +849,7 @@ static std::vector<Item> host_expand(unsigned n, const std::vector<Item>& in, un
 
 struct Contraction {
   u128 count = 0;
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
   u64 peak_states = 1;
   std::vector<RowAcc> rows;
   RunStats rs;
@@ -934,8 +939,20 @@ static double serve_estimate(unsigned n, unsigned k) {
   return std::max(e, 1.0);
 }
 
+static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
+                          Contraction& out);
+
+// Contraction plus the host<->device bytes it moved.
 static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
                      Contraction& out) {
+  const uint64_t h0 = ctx.h2d_bytes, d0 = ctx.d2h_bytes;
+  contract_impl(ctx, n, o, prefix, k, out);
+  out.h2d_bytes = ctx.h2d_bytes - h0;
+  out.d2h_bytes = ctx.d2h_bytes - d0;
+}
+
+static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
+                          Contraction& out) {
   auto t0 = std::chrono::steady_clock::now();
   if (n > 42) fail(QPEPS_ERR_RANGE, "the packed u128 virtual-boundary backend supports N <= 42");
   out.rows.assign(n, RowAcc());
@@ -1094,6 +1111,8 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->tail_items = c.rs.tail_items;
   r->tail_overflow = c.rs.tail_overflow;
   r->tail_kernel_ms = c.rs.tail_ms;
+  r->h2d_bytes = c.h2d_bytes;
+  r->d2h_bytes = c.d2h_bytes;
   for (int i = 0; i < kMaxResidues; ++i) {
     r->residue_primes[i] = i < (n ? c.plan.R : 0) ? kPrimes[i] : 0;
     r->count_residues[i] = i < (n ? c.plan.R : 0) ? (uint64_t)(c.count % kPrimes[i]) : 0;
