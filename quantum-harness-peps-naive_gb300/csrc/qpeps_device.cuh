@@ -32,6 +32,24 @@ __host__ __device__ __forceinline__ u32 add_mod(u32 a, u32 b, u32 p) {
   return s >= p ? s - p : s;
 }
 
+// The residue primes are 2^31 - c with c = 1, 19, 61, 69. For x < 2^52 (a sum
+// of up to 2^21 residues), (x & (2^31-1)) + c * (x >> 31) is congruent to x and
+// below 2p, so one conditional subtraction of p finishes the reduction.
+__host__ __device__ __forceinline__ constexpr u32 prime_gap(int r) {
+  return r == 0 ? 1u : r == 1 ? 19u : r == 2 ? 61u : 69u;
+}
+__host__ __device__ __forceinline__ u32 reduce_sum(u64 x, int r) {
+  const u64 y = (x & 0x7fffffffull) + (u64)prime_gap(r) * (x >> 31);
+  const u32 p = 0x80000000u - prime_gap(r);
+  return (u32)(y >= p ? y - p : y);
+}
+
+// Fibonacci hashing (Knuth, multiplicative): the high bits of key * odd
+// constant. Two different multipliers give independent partition and slot
+// indices.
+__host__ __device__ __forceinline__ u64 fib_hash_a(u64 k) { return k * 0x9E3779B97F4A7C15ull; }
+__host__ __device__ __forceinline__ u64 fib_hash_b(u64 k) { return k * 0xD6E8FEB86659FD93ull; }
+
 __host__ __device__ __forceinline__ u32 mul_mod(u32 a, u32 b, u32 p) {
   return (u32)(((u64)a * (u64)b) % p);
 }

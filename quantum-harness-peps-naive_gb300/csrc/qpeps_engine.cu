@@ -15,6 +15,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -274,6 +275,10 @@ struct Ctx {
   bool c_uploaded = false;
   double partition_fill = 0.83;  // target candidates per partition / partition slots
   uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued (since context creation)
+  struct Tune {
+    uint32_t parents_per_lane = 4;              // partition scatter: 2 or 4
+    uint32_t spread_cursors_below = 262144;     // pad cursors to 32 B when partitions <= this
+  } tune;
   DevBuf tail;                   // TailControl + overflow list
 };
 
@@ -334,6 +339,8 @@ static Ctx* ctx_create(int device) {
     size_t fr = 0, tot = 0;
     cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
     ctx->free_at_create = fr;
+    if (const char* e = std::getenv("QPEPS_SCATTER_PPL")) ctx->tune.parents_per_lane = std::atoi(e) == 4 ? 4 : 2;
+    if (const char* e = std::getenv("QPEPS_SPREAD_CURSORS_BELOW")) ctx->tune.spread_cursors_below = (uint32_t)std::atoi(e);
     ctx->c = build_c_sec_vi();
     certify_c(ctx->c);
     ctx->c_dev = c_table_for_device(ctx->c);
@@ -505,7 +512,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   const u32 pcap = partition_capacity();
   double mean = ctx.partition_fill * pcap;
   for (int attempt = 0;; ++attempt) {
-    u32 parts = 0;
+    u32 parts = 0, cstride = 1;
     u64 slots = 0;
     size_t table_bytes, region_bytes = 0;
     if (partition) {
@@ -513,7 +520,8 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
       if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
       parts = (u32)parts64;
       region_bytes = (size_t)parts * pcap * candidate_bytes(p.R);
-      table_bytes = region_bytes + ((size_t)parts * 4 + 255) / 256 * 256;
+      cstride = (parts <= ctx.tune.spread_cursors_below) ? 8u : 1u;
+      table_bytes = region_bytes + ((size_t)parts * 4 * cstride + 255) / 256 * 256;
     } else {
       slots = pow2_at_least(std::max<u64>(1024, so.terms * 2));
       table_bytes = slots * slot_bytes(p.key_bits, p.R);
@@ -538,11 +546,11 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     FrontierView view = view_of(p, ctx.front[0], f.cap);
     const u64 terms = so.terms;
     cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-    PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1};
+    PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane};
     void* regions = ctx.table.ptr;
     uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
     if (partition)
-      cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear partition cursors");
+      cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4 * cstride, ctx.stream), "clear partition cursors");
     else
       cuda_check(cudaMemsetAsync(ctx.table.ptr, 0, table_bytes, ctx.stream), "clear hash table");
     cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");

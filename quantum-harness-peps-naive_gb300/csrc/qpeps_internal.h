@@ -79,6 +79,8 @@ struct PartitionCfg {
   uint32_t parts;
   uint32_t cap;
   int merge_blocks_per_sm;
+  uint32_t cursor_stride = 1;     // u32 slots between partition cursors (1 or 8)
+  uint32_t parents_per_lane = 2;  // scatter: parents per lane per iteration (2 or 4)
 };
 
 size_t candidate_bytes(int residues);

@@ -106,15 +106,17 @@ __device__ __forceinline__ unsigned long long pblock_sum(unsigned long long v) {
 // up to KB*32 successors issues all cursor atomics before any store, so each
 // lane keeps KB atomics in flight.
 
-constexpr int kPPL = 2;  // parents per lane per iteration
-constexpr int kKB = 4;   // successor rounds per atomic batch
+constexpr int kKB = 4;  // successor rounds per atomic batch
 
-template <int R, int BLOCK, typename Layout>
+// kPPL parents per lane per iteration (2 or 4); partition cursors are
+// `cstride` u32 apart (a stride of 8 gives each cursor its own 32-byte sector,
+// spreading a small cursor array over more L2 slices).
+template <int R, int BLOCK, int kPPL, typename Layout>
 __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __restrict__ keys,
                                                                   const u32* __restrict__ res, u64 res_stride,
                                                                   u64 n_in, Layout L, Cand<R>* __restrict__ regions,
-                                                                  u32* __restrict__ cursors, u32 parts, u32 cap,
-                                                                  StepScalars* __restrict__ sc) {
+                                                                  u32* __restrict__ cursors, u32 cstride, u32 parts,
+                                                                  u32 cap, StepScalars* __restrict__ sc) {
   constexpr int WARPS = BLOCK / 32;
   constexpr int PW = 32 * kPPL;  // parents per warp iteration
   __shared__ u64 s_key[WARPS][PW];
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
   if (base < n_in) fetch(base);
   for (; base < n_in; base += stride) {
     int cnt = 0;
-    int c0 = 0;
+    int cum[kPPL];  // successors of this lane's parents 0..q-1
 #pragma unroll
     for (int q = 0; q < kPPL; ++q) {
       u64 fr = 0;
@@ -156,9 +158,8 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
       s_free[wid][q * 32 + lane] = fr;
 #pragma unroll
       for (int r = 0; r < R; ++r) s_w[wid][r][q * 32 + lane] = nw[q][r];
-      const int c = __popcll(fr);
-      if (q == 0) c0 = c;
-      cnt += c;
+      cum[q] = cnt;
+      cnt += __popcll(fr);
     }
     if (base + stride < n_in) fetch(base + stride);
     const int incl = pwarp_inclusive_scan(cnt);
@@ -170,6 +171,8 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
       u32 part[kKB], pos[kKB];
 #pragma unroll
       for (int k = 0; k < kKB; ++k) {
+        part[k] = 0xffffffffu;
+        if (j0 + k * 32 >= total) continue;  // warp-uniform: no successors left for this round
         const int j = j0 + k * 32 + lane;
         int owner = 0;
 #pragma unroll
@@ -178,12 +181,16 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
           if (v <= j) owner += step;
         }
         const int oex = __shfl_sync(kFullMask, excl, owner);
-        const int oc0 = __shfl_sync(kFullMask, c0, owner);
-        part[k] = 0xffffffffu;
+        int ocum[kPPL];
+#pragma unroll
+        for (int q = 1; q < kPPL; ++q) ocum[q] = __shfl_sync(kFullMask, cum[q], owner);
         if (j < total) {
           int t = j - oex;
-          const int q = t < oc0 ? 0 : 1;
-          if (q) t -= oc0;
+          int q = 0;
+#pragma unroll
+          for (int qq = 1; qq < kPPL; ++qq)
+            if (t >= ocum[qq]) q = qq;
+          t -= q ? ocum[q] : 0;
           const int slot = q * 32 + owner;
           const u64 pkey = s_key[wid][slot];
           const State s = L.unpack(pkey);
@@ -191,12 +198,12 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
           c[k].key = L.successor(pkey, s, 1ull << col);
 #pragma unroll
           for (int r = 0; r < R; ++r) c[k].res[r] = s_w[wid][r][slot];
-          part[k] = partition_of(mix64(c[k].key), parts);
+          part[k] = partition_of(fib_hash_a(c[k].key), parts);
         }
       }
 #pragma unroll
       for (int k = 0; k < kKB; ++k)
-        if (part[k] != 0xffffffffu) pos[k] = atomicAdd(&cursors[part[k]], 1u);
+        if (part[k] != 0xffffffffu) pos[k] = atomicAdd(&cursors[(u64)part[k] * cstride], 1u);
 #pragma unroll
       for (int k = 0; k < kKB; ++k)
         if (part[k] != 0xffffffffu) {
@@ -222,10 +229,13 @@ constexpr u64 kEmpty = kEmptyKey;
 
 template <int R, int BLOCK, int H, int CAP, typename Layout>
 __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* __restrict__ regions,
-                                                                const u32* __restrict__ cursors, u32 parts,
+                                                                const u32* __restrict__ cursors, u32 cstride,
+                                                                u32 parts,
                                                                 u64* __restrict__ keys_out, u32* __restrict__ res_out,
                                                                 u64 out_stride, Layout L, int write_out,
                                                                 StepScalars* __restrict__ sc) {
+  static_assert((H & (H - 1)) == 0 && H >= 2, "merge table size must be a power of two");
+  constexpr int kLogH = 31 - __builtin_clz(H);
   constexpr int WARPS = BLOCK / 32;
   constexpr int PER = H / BLOCK;    // table slots per thread
   constexpr int LPT = CAP / BLOCK;  // candidate loads per thread
@@ -257,7 +267,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   Cand<R> buf[LPT];
   u32 bcnt = 0;
   auto fetch = [&](u32 part) {
-    bcnt = min(cursors[part], (u32)CAP);
+    bcnt = min(cursors[(u64)part * cstride], (u32)CAP);
     const Cand<R>* src = regions + (u64)part * CAP;
 #pragma unroll
     for (int l = 0; l < LPT; ++l) {
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
       const u32 i = l * BLOCK + threadIdx.x;
       if (i < bcnt) {
         const Cand<R>& c = buf[l];
-        u32 slot = (u32)mix64(c.key) & (H - 1);
+        u32 slot = (u32)(fib_hash_b(c.key) >> (64 - kLogH));
         for (int probe = 0; probe < H; ++probe) {
           u64 cur = s_key[slot];
           if (cur == kEmpty) {
@@ -308,7 +318,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
           const int slot = it * BLOCK + threadIdx.x;
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            atomicAdd(&s_slot_fin[L.slot(key) * R + r], s_acc[r * H + slot] % prime_at(r));
+            atomicAdd(&s_slot_fin[L.slot(key) * R + r], (unsigned long long)reduce_sum(s_acc[r * H + slot], r));
             s_acc[r * H + slot] = 0ull;
           }
           s_key[slot] = kEmpty;
@@ -353,7 +363,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
         if (write_out) keys_out[idx] = key;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const u32 v = (u32)(s_acc[r * H + slot] % prime_at(r));
+          const u32 v = reduce_sum(s_acc[r * H + slot], r);
           if (write_out) res_out[r * out_stride + idx] = v;
           wsum[r] += v;
           if (full) fsum[r] += v;
@@ -405,16 +415,23 @@ constexpr size_t merge_smem() {
   return (size_t)kMergeH * (8 + 8 * R);
 }
 
+template <int R, int PPL, typename Layout>
+cudaError_t scatter_ppl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
+                        u32* cursors, StepScalars* sc, cudaStream_t stream) {
+  u64 want = (n_in + kScatterBlock * PPL - 1) / (kScatterBlock * PPL);
+  const u64 capb = (u64)pc.sms * 8;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
+  partition_scatter_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
+      reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
+      pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
+  return cudaGetLastError();
+}
+
 template <int R, typename Layout>
 cudaError_t scatter_impl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
                          u32* cursors, StepScalars* sc, cudaStream_t stream) {
-  u64 want = (n_in + kScatterBlock * kPPL - 1) / (kScatterBlock * kPPL);
-  const u64 capb = (u64)pc.sms * 8;
-  const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
-  partition_scatter_kernel<R, kScatterBlock, Layout><<<grid, kScatterBlock, 0, stream>>>(
-      reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
-      pc.parts, pc.cap, sc);
-  return cudaGetLastError();
+  if (pc.parents_per_lane == 4) return scatter_ppl<R, 4, Layout>(pc, in, n_in, L, regions, cursors, sc, stream);
+  return scatter_ppl<R, 2, Layout>(pc, in, n_in, L, regions, cursors, sc, stream);
 }
 
 template <int R, typename Layout>
@@ -426,7 +443,8 @@ cudaError_t merge_impl(const PartitionCfg& pc, const void* regions, const u32* c
   if (e != cudaSuccess) return e;
   const u64 capb = (u64)pc.sms * pc.merge_blocks_per_sm;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, capb));
-  kern<<<grid, kMergeBlock, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors, pc.parts,
+  kern<<<grid, kMergeBlock, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors,
+                                            pc.cursor_stride ? pc.cursor_stride : 1, pc.parts,
                                             reinterpret_cast<u64*>(out.keys), out.res, out.cap, L, write_out ? 1 : 0,
                                             sc);
   return cudaGetLastError();
