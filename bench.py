@@ -244,7 +244,7 @@ def run_ours(args):
     achieved = d["merge_kernel_bytes"] / max(d["device_ms"] / 1e3, 1e-12) / 1e9
     roofline = {
         "bound": "hbm",
-        "kernel": ("merge step: partition_scatter_kernel + partition_merge_kernel" if d["merge"] == 2
+        "kernel": ("merge step: partition_scatter_list_kernel + partition_merge_list_kernel" if d["merge"] == 2
                    else "merge step: row_expand_insert_kernel + compact_kernel (global table)"),
         "achieved": achieved,
         "peak": peak,

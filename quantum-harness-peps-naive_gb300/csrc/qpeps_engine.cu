@@ -278,6 +278,11 @@ struct Ctx {
   struct Tune {
     uint32_t parents_per_lane = 4;              // partition scatter: 2 or 4
     uint32_t spread_cursors_below = 262144;     // pad cursors to 32 B when partitions <= this
+    uint32_t wide_merge = 2;                    // 0 never, 1 always, 2 above wide_above_parts partitions:
+                                                // 8192-slot merge CTAs (4096-candidate partitions)
+    uint32_t wide_above_parts = 524288;         // 2048-candidate partitions beyond which auto goes wide
+    uint32_t scatter_kind = 1;                  // PartitionCfg::scatter_kind
+    uint32_t merge_kind = 1;                    // PartitionCfg::merge_kind
   } tune;
   DevBuf tail;                   // TailControl + overflow list
 };
@@ -341,6 +346,9 @@ static Ctx* ctx_create(int device) {
     ctx->free_at_create = fr;
     if (const char* e = std::getenv("QPEPS_SCATTER_PPL")) ctx->tune.parents_per_lane = std::atoi(e) == 4 ? 4 : 2;
     if (const char* e = std::getenv("QPEPS_SPREAD_CURSORS_BELOW")) ctx->tune.spread_cursors_below = (uint32_t)std::atoi(e);
+    if (const char* e = std::getenv("QPEPS_WIDE_MERGE")) ctx->tune.wide_merge = (uint32_t)std::atoi(e);
+    if (const char* e = std::getenv("QPEPS_SCATTER_KIND")) ctx->tune.scatter_kind = std::atoi(e) == 0 ? 0u : 1u;
+    if (const char* e = std::getenv("QPEPS_MERGE_KIND")) ctx->tune.merge_kind = std::atoi(e) == 0 ? 0u : 1u;
     ctx->c = build_c_sec_vi();
     certify_c(ctx->c);
     ctx->c_dev = c_table_for_device(ctx->c);
@@ -509,7 +517,13 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   }
   const bool partition = p.merge == QPEPS_MERGE_PARTITION && !site;
   const size_t eb = entry_bytes(p);
-  const u32 pcap = partition_capacity();
+  // Wide merge CTAs halve the number of open partition tails the scatter
+  // keeps in L2; they pay off once the narrow partitions no longer fit there.
+  const double narrow_parts = (double)so.terms / (ctx.partition_fill * partition_capacity(0));
+  const bool want_wide = ctx.tune.wide_merge == 1 ||
+                         (ctx.tune.wide_merge == 2 && narrow_parts > (double)ctx.tune.wide_above_parts);
+  const u32 wide = (want_wide && wide_merge_supported(p.R)) ? 1u : 0u;
+  const u32 pcap = partition_capacity(wide);
   double mean = ctx.partition_fill * pcap;
   for (int attempt = 0;; ++attempt) {
     u32 parts = 0, cstride = 1;
@@ -546,7 +560,8 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     FrontierView view = view_of(p, ctx.front[0], f.cap);
     const u64 terms = so.terms;
     cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-    PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane};
+    PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane,
+                    wide, ctx.tune.scatter_kind, ctx.tune.merge_kind};
     void* regions = ctx.table.ptr;
     uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
     if (partition)
@@ -1399,7 +1414,8 @@ static void serve_batch_loop(Server& sv) {
         buf_reserve(ctx, ctx.table, table_bytes, p.budget, "serve partitions");
         view = view_of(p, ctx.front[0], sv.f.cap);
         uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
-        PartitionCfg pc{2, ctx.sms, parts, pcap, 2};
+        PartitionCfg pc{2, ctx.sms, parts, pcap, 2, 1, ctx.tune.parents_per_lane, 0, ctx.tune.scatter_kind,
+                        ctx.tune.merge_kind};
         cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear cursors");
         cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
         cuda_check(launch_serve_scatter(pc, view, sv.f.count, d_mask, ctx.table.ptr, cursors, sc, ctx.stream),

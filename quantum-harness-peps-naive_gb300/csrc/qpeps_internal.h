@@ -81,10 +81,20 @@ struct PartitionCfg {
   int merge_blocks_per_sm;
   uint32_t cursor_stride = 1;     // u32 slots between partition cursors (1 or 8)
   uint32_t parents_per_lane = 2;  // scatter: parents per lane per iteration (2 or 4)
+  uint32_t wide = 0;              // merge CTA shape: 0 = 512 threads, 4096-slot table, 2048 candidates,
+                                  // two CTAs per SM; 1 = 1024 threads, 8192 slots, 4096 candidates,
+                                  // one CTA per SM (R <= 2 only: the table is 8 KiB x (8 + 8R) bytes)
+  uint32_t scatter_kind = 1;      // scatter: 0 = shuffle search for each successor's parent,
+                                  // 1 = per-warp shared-memory candidate window
+  uint32_t merge_kind = 1;        // merge: 0 = ballot/scan compaction over the whole table,
+                                  // 1 = claim list + first-claimant stores (three phases)
 };
 
 size_t candidate_bytes(int residues);
-uint32_t partition_capacity();
+// Candidate slots per partition for a merge shape (PartitionCfg::wide).
+uint32_t partition_capacity(uint32_t wide = 0);
+// Whether the wide merge shape is available for a residue count.
+bool wide_merge_supported(int residues);
 
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* scalars, cudaStream_t stream);

@@ -218,6 +218,110 @@ __global__ void __launch_bounds__(BLOCK) partition_scatter_kernel(const u64* __r
   if (overflow) atomicOr(&sc->error, kErrOverflow);
 }
 
+// List-expansion variant of the scatter. Each lane keeps its kPPL parents in
+// registers and writes its own successors, as finished 16- or 32-byte
+// candidates, into a per-warp shared-memory window of kKB*32 slots (lane
+// order = scan order, so the window is dense); the warp then reads the window
+// back one candidate per lane and round, and issues the cursor atomics and
+// stores. No shuffle search and no nth-set-bit: every successor is produced
+// by the lane that owns its parent, lowest free column first. Same inputs,
+// outputs and overflow rule as partition_scatter_kernel.
+template <int R, int BLOCK, int kPPL, typename Layout>
+__global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_list_kernel(const u64* __restrict__ keys,
+                                                                       const u32* __restrict__ res, u64 res_stride,
+                                                                       u64 n_in, Layout L,
+                                                                       Cand<R>* __restrict__ regions,
+                                                                       u32* __restrict__ cursors, u32 cstride,
+                                                                       u32 parts, u32 cap,
+                                                                       StepScalars* __restrict__ sc) {
+  constexpr int WARPS = BLOCK / 32;
+  constexpr int PW = 32 * kPPL;  // parents per warp iteration
+  constexpr int WIN = 32 * kKB;  // candidates per window
+  __shared__ Cand<R> s_cand[WARPS][WIN];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const u64 gwarp = (u64)blockIdx.x * WARPS + wid;
+  const u64 stride = (u64)gridDim.x * WARPS * PW;
+  bool overflow = false;
+
+  u64 nkey[kPPL], ckey[kPPL], fr[kPPL];
+  u32 nw[kPPL][R], cw[kPPL][R];
+  auto fetch = [&](u64 base) {
+#pragma unroll
+    for (int q = 0; q < kPPL; ++q) {
+      const u64 i = base + q * 32 + lane;
+      nkey[q] = kEmptyKey;
+      if (i < n_in) {
+        nkey[q] = keys[i];
+#pragma unroll
+        for (int r = 0; r < R; ++r) nw[q][r] = res[r * res_stride + i];
+      }
+    }
+  };
+  u64 base = gwarp * PW;
+  if (base < n_in) fetch(base);
+  for (; base < n_in; base += stride) {
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < kPPL; ++q) {
+      ckey[q] = nkey[q];
+      fr[q] = 0;
+      if (ckey[q] != kEmptyKey) {
+        const State s = L.unpack(ckey[q]);
+        fr[q] = ~(s.cols | s.dr | s.dl) & L.mask_of(ckey[q]);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) cw[q][r] = nw[q][r];
+      cnt += __popcll(fr[q]);
+    }
+    if (base + stride < n_in) fetch(base + stride);
+    const int incl = pwarp_inclusive_scan(cnt);
+    const int total = __shfl_sync(kFullMask, incl, 31);
+    int g = incl - cnt;  // index of this lane's next successor
+    for (int j0 = 0; j0 < total; j0 += WIN) {
+      const int hi = min(incl, j0 + WIN);
+#pragma unroll
+      for (int q = 0; q < kPPL; ++q) {
+        if (g < hi && fr[q]) {
+          const State s = L.unpack(ckey[q]);
+          do {
+            const u64 b = fr[q] & (0ull - fr[q]);
+            fr[q] ^= b;
+            Cand<R> c;
+            c.key = L.successor(ckey[q], s, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) c.res[r] = cw[q][r];
+            s_cand[wid][g - j0] = c;
+            ++g;
+          } while (g < hi && fr[q]);
+        }
+      }
+      __syncwarp();
+      // Candidates stay in shared memory while their cursor atomics are in
+      // flight (only the partition index is held in registers).
+      u32 part[kKB], pos[kKB];
+#pragma unroll
+      for (int k = 0; k < kKB; ++k) {
+        part[k] = 0xffffffffu;
+        if (j0 + k * 32 + lane < total)
+          part[k] = partition_of(fib_hash_a(s_cand[wid][k * 32 + lane].key), parts);
+      }
+#pragma unroll
+      for (int k = 0; k < kKB; ++k)
+        if (part[k] != 0xffffffffu) pos[k] = atomicAdd(&cursors[(u64)part[k] * cstride], 1u);
+#pragma unroll
+      for (int k = 0; k < kKB; ++k)
+        if (part[k] != 0xffffffffu) {
+          if (pos[k] < cap)
+            store_cand<R>(regions + (u64)part[k] * cap + pos[k], s_cand[wid][k * 32 + lane]);
+          else
+            overflow = true;
+        }
+      __syncwarp();
+    }
+  }
+  if (overflow) atomicOr(&sc->error, kErrOverflow);
+}
+
 // ---------------------------------------------------------------------------
 // Merge. One CTA per partition at a time (persistent over partitions). All
 // candidate loads of a partition are issued together into registers; the
@@ -391,6 +495,167 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   }
 }
 
+// Listed variant of the merge, in three phases per partition:
+//   1. every candidate claims or finds its key's slot with one shared-memory
+//      compare-and-swap; a key's first claimant appends the slot to a list
+//      (one shared atomic per warp);
+//   2. (after a barrier) first claimants store their residues into the
+//      accumulators, so those need no zeroing and most candidates (keys seen
+//      once) cost no atomic addition;
+//   3. (after a barrier) the remaining candidates add their residues.
+// Compaction then walks only the listed slots, and the list index is the
+// output index (no ballot/scan pass over the table). In the slotted (serving)
+// layout a finished board is summed into its request slot in phase 1 and never
+// enters the table. Same inputs, outputs and sums as partition_merge_kernel;
+// the order of the written entries differs.
+template <int R, int BLOCK, int H, int CAP, typename Layout>
+__global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<R>* __restrict__ regions,
+                                                                     const u32* __restrict__ cursors, u32 cstride,
+                                                                     u32 parts, u64* __restrict__ keys_out,
+                                                                     u32* __restrict__ res_out, u64 out_stride,
+                                                                     Layout L, int write_out,
+                                                                     StepScalars* __restrict__ sc) {
+  static_assert((H & (H - 1)) == 0 && H >= 2 * CAP, "merge table size must be a power of two >= 2 CAP");
+  constexpr int kLogH = 31 - __builtin_clz(H);
+  constexpr int LPT = CAP / BLOCK;  // candidate loads per thread
+  static_assert(CAP % BLOCK == 0, "shape");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u64* s_key = reinterpret_cast<u64*>(smem_raw);
+  unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [R][H]
+  u32* s_list = reinterpret_cast<u32*>(smem_raw + sizeof(u64) * H * (1 + R));                    // [CAP]
+  __shared__ u32 s_nused, s_n;
+  __shared__ unsigned long long s_base;
+  __shared__ unsigned long long s_slot_fin[Layout::kSlotted ? kServeMaxSlots * R : 1];
+  const int lane = threadIdx.x & 31;
+  if constexpr (Layout::kSlotted)
+    for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK) s_slot_fin[i] = 0ull;
+  if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
+  unsigned long long wsum[R], fsum[R], fstates = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
+  for (int i = threadIdx.x; i < H; i += BLOCK) {
+    s_key[i] = kEmpty;
+#pragma unroll
+    for (int r = 0; r < R; ++r) s_acc[r * H + i] = 0ull;
+  }
+  if (threadIdx.x == 0) s_nused = 0;
+
+  Cand<R> buf[LPT];
+  u32 bcnt = 0;
+  auto fetch = [&](u32 part) {
+    bcnt = min(cursors[(u64)part * cstride], (u32)CAP);
+    const Cand<R>* src = regions + (u64)part * CAP;
+#pragma unroll
+    for (int l = 0; l < LPT; ++l) {
+      const u32 i = l * BLOCK + threadIdx.x;
+      if (i < bcnt) buf[l] = load_cand<R>(src + i);
+    }
+  };
+  u32 part = blockIdx.x;
+  if (part < parts) fetch(part);
+  __syncthreads();
+  for (; part < parts; part += gridDim.x) {
+    u32 slots[LPT];
+    u32 fresh_bits = 0, dup_bits = 0;
+#pragma unroll
+    for (int l = 0; l < LPT; ++l) {
+      const u32 i = l * BLOCK + threadIdx.x;
+      bool fresh = false;
+      u32 slot = 0;
+      if (i < bcnt) {
+        const Cand<R>& c = buf[l];
+        bool finished = false;
+        if constexpr (Layout::kSlotted) {
+          const u64 m = L.mask_of(c.key);
+          if ((c.key & m) == m) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) atomicAdd(&s_slot_fin[L.slot(c.key) * R + r], (unsigned long long)c.res[r]);
+            finished = true;
+          }
+        }
+        if (!finished) {
+          slot = (u32)(fib_hash_b(c.key) >> (64 - kLogH));
+          for (int probe = 0; probe < H; ++probe) {
+            const u64 cur = atomicCAS(reinterpret_cast<unsigned long long*>(&s_key[slot]), kEmpty, c.key);
+            if (cur == kEmpty || cur == c.key) {
+              fresh = cur == kEmpty;
+              dup_bits |= (u32)(!fresh) << l;
+              break;
+            }
+            slot = (slot + 1) & (H - 1);
+          }
+        }
+      }
+      slots[l] = slot;
+      fresh_bits |= (u32)fresh << l;
+      const u32 b = __ballot_sync(kFullMask, fresh);
+      if (b) {
+        const int leader = __ffs(b) - 1;
+        u32 at = 0;
+        if (lane == leader) at = atomicAdd(&s_nused, (u32)__popc(b));
+        at = __shfl_sync(kFullMask, at, leader);
+        if (fresh) s_list[at + __popc(b & ((1u << lane) - 1u))] = slot;
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < LPT; ++l)
+      if ((fresh_bits >> l) & 1u) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) s_acc[r * H + slots[l]] = buf[l].res[r];
+      }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < LPT; ++l)
+      if ((dup_bits >> l) & 1u) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slots[l]], (unsigned long long)buf[l].res[r]);
+      }
+    __syncthreads();
+    const u32 next = part + gridDim.x;
+    if (next < parts) fetch(next);
+    if (threadIdx.x == 0) {
+      const u32 n = s_nused;
+      s_n = n;
+      s_base = n ? atomicAdd(&sc->out_count, (unsigned long long)n) : 0ull;
+      s_nused = 0;
+    }
+    __syncthreads();
+    const u32 n = s_n;
+    const unsigned long long base = s_base;
+    for (u32 i = threadIdx.x; i < n; i += BLOCK) {
+      const u32 slot = s_list[i];
+      const u64 key = s_key[slot];
+      const u64 idx = base + i;
+      const bool full = (key & L.mask_of(key)) == L.mask_of(key);
+      if (write_out) keys_out[idx] = key;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const u32 v = reduce_sum(s_acc[r * H + slot], r);
+        if (write_out) res_out[r * out_stride + idx] = v;
+        wsum[r] += v;
+        if (full) fsum[r] += v;
+      }
+      s_key[slot] = kEmpty;
+      fstates += full;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    unsigned long long t = pblock_sum<BLOCK>(wsum[r]);
+    if (threadIdx.x == 0 && t) atomicAdd(&sc->weight_sum[r], t);
+    t = pblock_sum<BLOCK>(fsum[r]);
+    if (threadIdx.x == 0 && t) atomicAdd(&sc->final_sum[r], t);
+  }
+  const unsigned long long t = pblock_sum<BLOCK>(fstates);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+  if constexpr (Layout::kSlotted) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK)
+      if (s_slot_fin[i]) atomicAdd(&L.slot_final[(i / R) * 4 + (i % R)], s_slot_fin[i]);
+  }
+}
+
 // Successor count of a slotted (serving) boundary.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) slot_count_kernel(const u64* __restrict__ keys, u64 n_in, SlotLayout L,
@@ -406,13 +671,13 @@ __global__ void __launch_bounds__(BLOCK) slot_count_kernel(const u64* __restrict
 }
 
 constexpr int kScatterBlock = 256;
-constexpr int kMergeBlock = 512;
-constexpr int kMergeH = 4096;
-constexpr int kMergeCap = kMergeH / 2;
+// Merge CTA shapes: table slots H, candidate capacity H / 2.
+constexpr int kMergeBlock = 512, kMergeH = 4096;
+constexpr int kWideBlock = 1024, kWideH = 8192;
 
-template <int R>
+template <int R, int H>
 constexpr size_t merge_smem() {
-  return (size_t)kMergeH * (8 + 8 * R);
+  return (size_t)H * (8 + 8 * R);
 }
 
 template <int R, int PPL, typename Layout>
@@ -421,6 +686,12 @@ cudaError_t scatter_ppl(const PartitionCfg& pc, const FrontierView& in, u64 n_in
   u64 want = (n_in + kScatterBlock * PPL - 1) / (kScatterBlock * PPL);
   const u64 capb = (u64)pc.sms * 8;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
+  if (pc.scatter_kind == 1) {
+    partition_scatter_list_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
+        reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
+        pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
+    return cudaGetLastError();
+  }
   partition_scatter_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
       reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
       pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
@@ -434,20 +705,34 @@ cudaError_t scatter_impl(const PartitionCfg& pc, const FrontierView& in, u64 n_i
   return scatter_ppl<R, 2, Layout>(pc, in, n_in, L, regions, cursors, sc, stream);
 }
 
+template <int R, int BLOCK, int H, typename Layout>
+cudaError_t merge_shape(const PartitionCfg& pc, int blocks_per_sm, const void* regions, const u32* cursors,
+                        const FrontierView& out, Layout L, bool write_out, StepScalars* sc, cudaStream_t stream) {
+  if (pc.cap != (u32)(H / 2)) return cudaErrorInvalidValue;
+  auto kern = pc.merge_kind == 1 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>
+                                 : partition_merge_kernel<R, BLOCK, H, H / 2, Layout>;
+  const size_t smem = merge_smem<R, H>() + (pc.merge_kind == 1 ? (size_t)(H / 2) * 4 : 0);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const u64 capb = (u64)pc.sms * blocks_per_sm;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, capb));
+  kern<<<grid, BLOCK, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors,
+                                      pc.cursor_stride ? pc.cursor_stride : 1, pc.parts,
+                                      reinterpret_cast<u64*>(out.keys), out.res, out.cap, L, write_out ? 1 : 0, sc);
+  return cudaGetLastError();
+}
+
 template <int R, typename Layout>
 cudaError_t merge_impl(const PartitionCfg& pc, const void* regions, const u32* cursors, const FrontierView& out,
                        Layout L, bool write_out, StepScalars* sc, cudaStream_t stream) {
-  auto kern = partition_merge_kernel<R, kMergeBlock, kMergeH, kMergeCap, Layout>;
-  const size_t smem = merge_smem<R>();
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const u64 capb = (u64)pc.sms * pc.merge_blocks_per_sm;
-  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, capb));
-  kern<<<grid, kMergeBlock, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors,
-                                            pc.cursor_stride ? pc.cursor_stride : 1, pc.parts,
-                                            reinterpret_cast<u64*>(out.keys), out.res, out.cap, L, write_out ? 1 : 0,
-                                            sc);
-  return cudaGetLastError();
+  if constexpr (R <= 2) {
+    if (pc.wide)
+      return merge_shape<R, kWideBlock, kWideH, Layout>(pc, 1, regions, cursors, out, L, write_out, sc, stream);
+  } else {
+    if (pc.wide) return cudaErrorInvalidValue;
+  }
+  return merge_shape<R, kMergeBlock, kMergeH, Layout>(pc, pc.merge_blocks_per_sm, regions, cursors, out, L,
+                                                      write_out, sc, stream);
 }
 
 }  // namespace
@@ -478,7 +763,8 @@ cudaError_t launch_serve_merge(const PartitionCfg& pc, const void* regions, cons
   if (pc.residues != 2) return cudaErrorInvalidValue;
   return merge_impl<2>(pc, regions, cursors, out, SlotLayout{slot_mask, slot_final}, true, sc, stream);
 }
-uint32_t partition_capacity() { return kMergeCap; }
+uint32_t partition_capacity(uint32_t wide) { return wide ? kWideH / 2 : kMergeH / 2; }
+bool wide_merge_supported(int residues) { return residues >= 1 && residues <= 2; }
 
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
