@@ -173,6 +173,42 @@ int qpeps_count_batch(void* ctx, uint32_t num, const uint32_t* n, const uint32_t
  * own C. */
 int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len);
 
+/* ---- Tuning ---------------------------------------------------------------
+ * No reference counterpart (the reference has one CPU code path): the knobs of
+ * the partitioned merge, held per context. Every setting gives the same
+ * counts and metrics; only the speed changes. */
+#define QPEPS_SCATTER_SEARCH 0 /* shuffle search for each successor's parent */
+#define QPEPS_SCATTER_WINDOW 1 /* per-warp shared-memory candidate window (default) */
+#define QPEPS_MERGEK_SCAN 0    /* ballot/scan compaction over the whole table */
+#define QPEPS_MERGEK_CLAIM 1   /* claim list + first-claimant stores (default) */
+
+typedef struct qpeps_tuning {
+  uint32_t struct_size;          /* sizeof(qpeps_tuning) */
+  uint32_t scatter_kind;         /* QPEPS_SCATTER_* */
+  uint32_t parents_per_lane;     /* scatter: parents per lane per warp iteration, 2 or 4 */
+  uint32_t merge_kind;           /* QPEPS_MERGEK_* */
+  uint32_t wide_merge;           /* 0 never, 1 always, 2 auto: 8192-slot merge CTAs, 4096-candidate partitions */
+  uint32_t wide_above_parts;     /* auto: 2048-candidate partition count above which merges go wide */
+  uint32_t spread_cursors_below; /* partition counts up to which cursors get 32-byte spacing */
+  uint32_t reserved;
+  double partition_fill;         /* mean candidates per partition / capacity, in [0.3, 0.95] */
+  double slice_margin;           /* predictive slicing: assumed slice peak / mean slice peak, >= 1 */
+} qpeps_tuning;
+
+/* Library defaults (what a new context starts with). */
+void qpeps_tuning_default(qpeps_tuning* t);
+int qpeps_ctx_get_tuning(void* ctx, qpeps_tuning* out);
+/* QPEPS_ERR_INVALID for an out-of-range field (the context keeps its tuning). */
+int qpeps_ctx_set_tuning(void* ctx, const qpeps_tuning* t, char* err, size_t err_len);
+/* Autotuner: time contract_rows(n) (8 <= n <= 18) under each tuning of a
+ * grid over scatter kind, parents per lane, merge kind and partition fill
+ * (device time, best of `repeats`; every count checked against
+ * known_count), keep the fastest in the context and return it. */
+int qpeps_autotune(void* ctx, uint32_t n, uint32_t repeats, qpeps_tuning* best, double* best_device_ms, char* err,
+                   size_t err_len);
+/* Name of the context's CUDA device (for keying tuning caches). */
+int qpeps_ctx_device_name(void* ctx, char* out, size_t len);
+
 /* ---- Serving: continuous batching of counting requests -------------------
  * No single reference counterpart: each request is the prefix contraction of
  * qpeps_count (contract_rows, src/lib.rs:758, from a placed prefix). A server

@@ -40,6 +40,10 @@ GRAIN_SITE = 1
 MERGE_AUTO = 0
 MERGE_HASH = 1
 MERGE_PARTITION = 2
+SCATTER_SEARCH = 0
+SCATTER_WINDOW = 1
+MERGEK_SCAN = 0
+MERGEK_CLAIM = 1
 
 
 class U128(ctypes.Structure):
@@ -152,6 +156,24 @@ class ServeStats(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in ("submitted", "completed", "batch_steps", "cache_hits", "large_runs")]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("scatter_kind", ctypes.c_uint32),
+        ("parents_per_lane", ctypes.c_uint32),
+        ("merge_kind", ctypes.c_uint32),
+        ("wide_merge", ctypes.c_uint32),
+        ("wide_above_parts", ctypes.c_uint32),
+        ("spread_cursors_below", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("partition_fill", ctypes.c_double),
+        ("slice_margin", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f not in ("struct_size", "reserved")}
+
+
 # Every symbol include/qpeps.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 _SIGNATURES = {
@@ -197,6 +219,15 @@ _SIGNATURES = {
     ),
     "qpeps_serve_stats_get": (ctypes.c_int, [_VP, ctypes.POINTER(ServeStats)]),
     "qpeps_serve_close": (None, [_VP]),
+    "qpeps_tuning_default": (None, [ctypes.POINTER(Tuning)]),
+    "qpeps_ctx_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
+    "qpeps_ctx_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning), ctypes.c_char_p, ctypes.c_size_t]),
+    "qpeps_autotune": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_double),
+         ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "qpeps_ctx_device_name": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_size_t]),
     "qpeps_certify_c": (
         ctypes.c_int,
         [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_char_p,
@@ -417,6 +448,75 @@ class Context:
             rc = lib.qpeps_count_batch(self._h, num, ns, ks, po, pc, ctypes.byref(o), counts, err, len(err))
         _check(rc, err)
         return [counts[i].value for i in range(num)]
+
+
+    # ---- tuning (no reference counterpart) ---------------------------------
+    @property
+    def tuning(self) -> dict:
+        t = Tuning()
+        rc = library().qpeps_ctx_get_tuning(self._h, ctypes.byref(t))
+        if rc != QPEPS_OK:
+            raise ContractionError(rc, "qpeps_ctx_get_tuning failed")
+        return t.as_dict()
+
+    def set_tuning(self, **kw) -> dict:
+        """Change tuning fields (see ``qpeps_tuning``); returns the new tuning."""
+        t = Tuning()
+        library().qpeps_ctx_get_tuning(self._h, ctypes.byref(t))
+        for k, v in kw.items():
+            if k not in t.as_dict():
+                raise ContractionError(QPEPS_ERR_INVALID, f"unknown tuning field {k}")
+            setattr(t, k, v)
+        err = ctypes.create_string_buffer(512)
+        with self._lock:
+            rc = library().qpeps_ctx_set_tuning(self._h, ctypes.byref(t), err, len(err))
+        _check(rc, err)
+        return self.tuning
+
+    @property
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        library().qpeps_ctx_device_name(self._h, buf, len(buf))
+        return buf.value.decode(errors="replace")
+
+    def autotune(self, n: int = 16, repeats: int = 2, cache: str | Path | None = None) -> dict:
+        """Pick the fastest tuning for this device (``qpeps_autotune`` on a
+        probe contraction of size ``n``). With ``cache``, a JSON file keyed
+        by device name, library version and ``n`` is read first and updated
+        after a search. Returns ``{"tuning": {...}, "device_ms": ms,
+        "cached": bool}``."""
+        import json
+
+        key = f"{self.device_name}|{version()}|n={int(n)}"
+        path = Path(cache) if cache is not None else None
+        entries = {}
+        if path is not None and path.exists():
+            try:
+                entries = json.loads(path.read_text())
+            except (OSError, ValueError):
+                entries = {}
+            if key in entries:
+                self.set_tuning(**entries[key]["tuning"])
+                return {"tuning": self.tuning, "device_ms": entries[key]["device_ms"], "cached": True}
+        t = Tuning()
+        ms = ctypes.c_double()
+        err = ctypes.create_string_buffer(512)
+        with self._lock:
+            rc = library().qpeps_autotune(self._h, int(n), int(repeats), ctypes.byref(t), ctypes.byref(ms), err,
+                                          len(err))
+        _check(rc, err)
+        out = {"tuning": t.as_dict(), "device_ms": ms.value, "cached": False}
+        if path is not None:
+            entries[key] = {"tuning": out["tuning"], "device_ms": out["device_ms"]}
+            path.write_text(json.dumps(entries, indent=1, sort_keys=True))
+        return out
+
+
+def tuning_default() -> dict:
+    """The library's default tuning (``qpeps_tuning_default``)."""
+    t = Tuning()
+    library().qpeps_tuning_default(ctypes.byref(t))
+    return t.as_dict()
 
 
 class Server:

@@ -273,7 +273,7 @@ struct Ctx {
   std::vector<CEntryH> c;
   CTableDev c_dev;
   bool c_uploaded = false;
-  double partition_fill = 0.83;  // target candidates per partition / partition slots
+  double partition_fill = 0.83;  // live target candidates per partition / slots (lowered after an overflow)
   uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued (since context creation)
   struct Tune {
     uint32_t parents_per_lane = 4;              // partition scatter: 2 or 4
@@ -283,6 +283,8 @@ struct Ctx {
     uint32_t wide_above_parts = 524288;         // 2048-candidate partitions beyond which auto goes wide
     uint32_t scatter_kind = 1;                  // PartitionCfg::scatter_kind
     uint32_t merge_kind = 1;                    // PartitionCfg::merge_kind
+    double partition_fill = 0.83;               // starting value of Ctx::partition_fill
+    double slice_margin = 2.0;                  // predictive slicing: slice peak / mean slice peak
   } tune;
   DevBuf tail;                   // TailControl + overflow list
 };
@@ -344,11 +346,6 @@ static Ctx* ctx_create(int device) {
     size_t fr = 0, tot = 0;
     cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
     ctx->free_at_create = fr;
-    if (const char* e = std::getenv("QPEPS_SCATTER_PPL")) ctx->tune.parents_per_lane = std::atoi(e) == 4 ? 4 : 2;
-    if (const char* e = std::getenv("QPEPS_SPREAD_CURSORS_BELOW")) ctx->tune.spread_cursors_below = (uint32_t)std::atoi(e);
-    if (const char* e = std::getenv("QPEPS_WIDE_MERGE")) ctx->tune.wide_merge = (uint32_t)std::atoi(e);
-    if (const char* e = std::getenv("QPEPS_SCATTER_KIND")) ctx->tune.scatter_kind = std::atoi(e) == 0 ? 0u : 1u;
-    if (const char* e = std::getenv("QPEPS_MERGE_KIND")) ctx->tune.merge_kind = std::atoi(e) == 0 ? 0u : 1u;
     ctx->c = build_c_sec_vi();
     certify_c(ctx->c);
     ctx->c_dev = c_table_for_device(ctx->c);
@@ -1038,8 +1035,8 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
     const double cap_states = 0.8 * (double)out.plan.budget / per_state;
     double est_total = serve_estimate(n, k);
     while (est_total > cap_states && row0 + 2 < n) {
-      // Slices are uneven (centre columns carry more states): margin 2.
-      const double est_item = est_total / (double)items.size() * 2.0;
+      // Slices are uneven (centre columns carry more states): tuned margin.
+      const double est_item = est_total / (double)items.size() * ctx.tune.slice_margin;
       if (est_item <= cap_states) {
         const size_t per_chunk = std::max<size_t>(1, (size_t)(cap_states / est_item));
         std::vector<HostChunk> chunks;
@@ -1515,6 +1512,93 @@ static void serve_thread_main(Server& sv, bool large) {
 
 using namespace qpeps;
 
+// ---- tuning --------------------------------------------------------------
+
+static qpeps_tuning tuning_of(const Ctx::Tune& t) {
+  qpeps_tuning q;
+  std::memset(&q, 0, sizeof q);
+  q.struct_size = sizeof(qpeps_tuning);
+  q.scatter_kind = t.scatter_kind;
+  q.parents_per_lane = t.parents_per_lane;
+  q.merge_kind = t.merge_kind;
+  q.wide_merge = t.wide_merge;
+  q.wide_above_parts = t.wide_above_parts;
+  q.spread_cursors_below = t.spread_cursors_below;
+  q.partition_fill = t.partition_fill;
+  q.slice_margin = t.slice_margin;
+  return q;
+}
+
+static Ctx::Tune tune_from(const qpeps_tuning& q) {
+  if (q.struct_size != sizeof(qpeps_tuning)) fail(QPEPS_ERR_INVALID, "qpeps_tuning.struct_size mismatch");
+  if (q.scatter_kind > 1) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0 or 1");
+  if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
+  if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
+  if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
+  if (!(q.partition_fill >= 0.3 && q.partition_fill <= 0.95))
+    fail(QPEPS_ERR_INVALID, "partition_fill must be in [0.3, 0.95]");
+  if (!(q.slice_margin >= 1.0 && q.slice_margin <= 64.0)) fail(QPEPS_ERR_INVALID, "slice_margin must be in [1, 64]");
+  Ctx::Tune t;
+  t.scatter_kind = q.scatter_kind;
+  t.parents_per_lane = q.parents_per_lane;
+  t.merge_kind = q.merge_kind;
+  t.wide_merge = q.wide_merge;
+  t.wide_above_parts = q.wide_above_parts;
+  t.spread_cursors_below = q.spread_cursors_below;
+  t.partition_fill = q.partition_fill;
+  t.slice_margin = q.slice_margin;
+  return t;
+}
+
+static void apply_tune(Ctx& c, const Ctx::Tune& t) {
+  c.tune = t;
+  c.partition_fill = t.partition_fill;
+}
+
+// Grid search over the knobs that change the kernels of every row step.
+static double autotune(Ctx& c, unsigned n, unsigned repeats, Ctx::Tune* best) {
+  if (n < 8 || n > 18) fail(QPEPS_ERR_RANGE, "autotune probe N must be in [8, 18]");
+  repeats = std::max(1u, std::min(repeats, 16u));
+  u128 known = 0;
+  known_count(n, &known);
+  qpeps_options o;
+  qpeps_options_default(&o);
+  o.collect_layers = 0;
+  const Ctx::Tune saved = c.tune;
+  double best_ms = 1e300;
+  Ctx::Tune best_t = saved;
+  try {
+    for (uint32_t sk : {1u, 0u})
+      for (uint32_t ppl : {4u, 2u})
+        for (uint32_t mk : {1u, 0u})
+          for (double fill : {0.83, 0.9, 0.75}) {
+            Ctx::Tune t = saved;
+            t.scatter_kind = sk;
+            t.parents_per_lane = ppl;
+            t.merge_kind = mk;
+            t.partition_fill = fill;
+            apply_tune(c, t);
+            double ms = 1e300;
+            for (unsigned r = 0; r <= repeats; ++r) {  // the first run warms buffers and is not timed
+              Contraction con;
+              contract(c, n, o, nullptr, 0, con);
+              if (con.count != known) fail(QPEPS_ERR_INVALID, "autotune: count differs from known_count");
+              if (r) ms = std::min(ms, con.rs.device_ms);
+            }
+            if (ms < best_ms) {
+              best_ms = ms;
+              best_t = t;
+            }
+          }
+  } catch (...) {
+    apply_tune(c, saved);
+    throw;
+  }
+  apply_tune(c, best_t);
+  *best = best_t;
+  return best_ms;
+}
+
 extern "C" {
 
 const char* qpeps_version(void) { return "qpeps-gb300 0.1.0 (sm_103a)"; }
@@ -1581,6 +1665,43 @@ int qpeps_count_batch(void* ctx, uint32_t num, const uint32_t* n, const uint32_t
       counts[i] = to_abi(con.count);
     }
   });
+}
+
+void qpeps_tuning_default(qpeps_tuning* t) { *t = tuning_of(Ctx::Tune{}); }
+
+int qpeps_ctx_get_tuning(void* ctx, qpeps_tuning* out) {
+  if (!ctx || !out) return QPEPS_ERR_INVALID;
+  Ctx& c = *static_cast<Ctx*>(ctx);
+  *out = tuning_of(c.tune);
+  out->partition_fill = c.partition_fill;
+  return QPEPS_OK;
+}
+
+int qpeps_ctx_set_tuning(void* ctx, const qpeps_tuning* t, char* err, size_t err_len) {
+  return guarded(err, err_len, [&] {
+    if (!ctx || !t) fail(QPEPS_ERR_INVALID, "null context or tuning");
+    apply_tune(*static_cast<Ctx*>(ctx), tune_from(*t));
+  });
+}
+
+int qpeps_autotune(void* ctx, uint32_t n, uint32_t repeats, qpeps_tuning* best, double* best_device_ms, char* err,
+                   size_t err_len) {
+  return guarded(err, err_len, [&] {
+    if (!ctx) fail(QPEPS_ERR_INVALID, "null context");
+    Ctx& c = *static_cast<Ctx*>(ctx);
+    Ctx::Tune t;
+    const double ms = autotune(c, n, repeats, &t);
+    if (best) *best = tuning_of(t);
+    if (best_device_ms) *best_device_ms = ms;
+  });
+}
+
+int qpeps_ctx_device_name(void* ctx, char* out, size_t len) {
+  if (!ctx || !out || !len) return QPEPS_ERR_INVALID;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, static_cast<Ctx*>(ctx)->device) != cudaSuccess) return QPEPS_ERR_CUDA;
+  std::snprintf(out, len, "%s", prop.name);
+  return QPEPS_OK;
 }
 
 int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len) {

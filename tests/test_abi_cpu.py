@@ -64,3 +64,13 @@ def test_certify_c_accepts_sec_vi_and_fails_closed(qp, oracle):
             qp.certify_c(table)
         assert ei.value.code == qp.QPEPS_ERR_INVALID
         assert oracle.compile_check(table) is not None
+
+
+def test_tuning_default_is_the_library_default(qp):
+    t = qp.tuning_default()
+    assert t["scatter_kind"] == qp.SCATTER_WINDOW
+    assert t["merge_kind"] == qp.MERGEK_CLAIM
+    assert t["parents_per_lane"] in (2, 4)
+    assert t["wide_merge"] == 2
+    assert 0.3 <= t["partition_fill"] <= 0.95
+    assert t["slice_margin"] >= 1.0

@@ -19,6 +19,7 @@ STRUCTS = {
     "qpeps_serve_config": "ServeConfig",
     "qpeps_serve_completion": "ServeCompletion",
     "qpeps_serve_stats": "ServeStats",
+    "qpeps_tuning": "Tuning",
 }
 
 
