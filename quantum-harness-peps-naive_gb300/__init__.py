@@ -165,13 +165,13 @@ class Tuning(ctypes.Structure):
         ("wide_merge", ctypes.c_uint32),
         ("wide_above_parts", ctypes.c_uint32),
         ("spread_cursors_below", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("fold_weights", ctypes.c_uint32),
         ("partition_fill", ctypes.c_double),
         ("slice_margin", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f not in ("struct_size", "reserved")}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "struct_size"}
 
 
 # Every symbol include/qpeps.h declares, with its ctypes signature.

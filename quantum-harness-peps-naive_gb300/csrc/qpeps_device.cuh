@@ -44,6 +44,30 @@ __host__ __device__ __forceinline__ u32 reduce_sum(u64 x, int r) {
   return (u32)(y >= p ? y - p : y);
 }
 
+// x mod prime_at(r) for any 64-bit x: two folds of the 2^31 - c form leave a
+// value below 2p, then one conditional subtraction.
+__host__ __device__ __forceinline__ u32 reduce_u64(u64 x, int r) {
+  const u64 c = prime_gap(r);
+  const u32 p = 0x80000000u - prime_gap(r);
+  u64 y = (x & 0x7fffffffull) + c * (x >> 31);
+  y = (y & 0x7fffffffull) + c * (y >> 31);
+  return (u32)(y >= p ? y - p : y);
+}
+
+// The value below p0 * p1 (< 2^62) with residues (r0 mod p0, r1 mod p1):
+// Garner's mixed-radix form of the Chinese remainder theorem,
+// value = r0 + p0 * ((r1 - r0) * p0^-1 mod p1).
+constexpr u32 kInvP0ModP1 = 2028178983u;
+static_assert(((unsigned long long)(prime_at(0) % prime_at(1)) * kInvP0ModP1) % prime_at(1) == 1,
+              "kInvP0ModP1 must invert p0 modulo p1");
+__host__ __device__ __forceinline__ u64 crt_fold2(u32 r0, u32 r1) {
+  constexpr u32 p1 = prime_at(1);
+  const u32 r0m = r0 >= p1 ? r0 - p1 : r0;
+  const u32 d = r1 >= r0m ? r1 - r0m : r1 + (p1 - r0m);
+  const u32 t = reduce_u64((u64)d * kInvP0ModP1, 1);
+  return (u64)r0 + (u64)prime_at(0) * t;
+}
+
 // Fibonacci hashing (Knuth, multiplicative): the high bits of key * odd
 // constant. Two different multipliers give independent partition and slot
 // indices.

@@ -283,6 +283,7 @@ struct Ctx {
     uint32_t wide_above_parts = 524288;         // 2048-candidate partitions beyond which auto goes wide
     uint32_t scatter_kind = 1;                  // PartitionCfg::scatter_kind
     uint32_t merge_kind = 1;                    // PartitionCfg::merge_kind
+    uint32_t fold_weights = 1;                  // PartitionCfg::fold where exact (R = 2, N <= 20)
     double partition_fill = 0.83;               // starting value of Ctx::partition_fill
     double slice_margin = 2.0;                  // predictive slicing: slice peak / mean slice peak
   } tune;
@@ -558,7 +559,8 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     const u64 terms = so.terms;
     cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
     PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane,
-                    wide, ctx.tune.scatter_kind, ctx.tune.merge_kind};
+                    wide, ctx.tune.scatter_kind, ctx.tune.merge_kind,
+                    (ctx.tune.fold_weights && p.R == 2 && p.n <= 20) ? 1u : 0u};
     void* regions = ctx.table.ptr;
     uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
     if (partition)
@@ -1412,7 +1414,7 @@ static void serve_batch_loop(Server& sv) {
         view = view_of(p, ctx.front[0], sv.f.cap);
         uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
         PartitionCfg pc{2, ctx.sms, parts, pcap, 2, 1, ctx.tune.parents_per_lane, 0, ctx.tune.scatter_kind,
-                        ctx.tune.merge_kind};
+                        ctx.tune.merge_kind, ctx.tune.fold_weights};  // serving boards have N <= 19
         cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear cursors");
         cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
         cuda_check(launch_serve_scatter(pc, view, sv.f.count, d_mask, ctx.table.ptr, cursors, sc, ctx.stream),
@@ -1524,6 +1526,7 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
   q.wide_merge = t.wide_merge;
   q.wide_above_parts = t.wide_above_parts;
   q.spread_cursors_below = t.spread_cursors_below;
+  q.fold_weights = t.fold_weights;
   q.partition_fill = t.partition_fill;
   q.slice_margin = t.slice_margin;
   return q;
@@ -1535,6 +1538,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
+  if (q.fold_weights > 1) fail(QPEPS_ERR_INVALID, "fold_weights must be 0 or 1");
   if (!(q.partition_fill >= 0.3 && q.partition_fill <= 0.95))
     fail(QPEPS_ERR_INVALID, "partition_fill must be in [0.3, 0.95]");
   if (!(q.slice_margin >= 1.0 && q.slice_margin <= 64.0)) fail(QPEPS_ERR_INVALID, "slice_margin must be in [1, 64]");
@@ -1545,6 +1549,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   t.wide_merge = q.wide_merge;
   t.wide_above_parts = q.wide_above_parts;
   t.spread_cursors_below = q.spread_cursors_below;
+  t.fold_weights = q.fold_weights;
   t.partition_fill = q.partition_fill;
   t.slice_margin = q.slice_margin;
   return t;

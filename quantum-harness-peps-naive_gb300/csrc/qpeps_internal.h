@@ -88,6 +88,8 @@ struct PartitionCfg {
                                   // 1 = per-warp shared-memory candidate window
   uint32_t merge_kind = 1;        // merge: 0 = ballot/scan compaction over the whole table,
                                   // 1 = claim list + first-claimant stores (three phases)
+  uint32_t fold = 0;              // merge_kind 1, R = 2: accumulate the CRT-folded value in one
+                                  // 64-bit plane (exact only when N! < p0 * p1, i.e. N <= 20)
 };
 
 size_t candidate_bytes(int residues);

@@ -508,7 +508,14 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
 // layout a finished board is summed into its request slot in phase 1 and never
 // enters the table. Same inputs, outputs and sums as partition_merge_kernel;
 // the order of the written entries differs.
-template <int R, int BLOCK, int H, int CAP, typename Layout>
+//
+// kFold (R = 2): a candidate's residue pair is folded into the one value
+// below p0 * p1 it stands for (crt_fold2) and keys accumulate that value in a
+// single 64-bit plane. This is exact when every weight and every sum of
+// weights stays below p0 * p1 (about 4.6e18) and 2^64: a row's weights sum to
+// at most the number of partial placements, at most N! (20! = 2.4e18), so the
+// engine folds for N <= 20.
+template <int R, int BLOCK, int H, int CAP, typename Layout, bool kFold = false>
 __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<R>* __restrict__ regions,
                                                                      const u32* __restrict__ cursors, u32 cstride,
                                                                      u32 parts, u64* __restrict__ keys_out,
@@ -519,10 +526,12 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   constexpr int kLogH = 31 - __builtin_clz(H);
   constexpr int LPT = CAP / BLOCK;  // candidate loads per thread
   static_assert(CAP % BLOCK == 0, "shape");
+  static_assert(!kFold || R == 2, "the folded accumulator holds one residue pair");
+  constexpr int AP = kFold ? 1 : R;  // accumulator planes
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* s_key = reinterpret_cast<u64*>(smem_raw);
-  unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [R][H]
-  u32* s_list = reinterpret_cast<u32*>(smem_raw + sizeof(u64) * H * (1 + R));                    // [CAP]
+  unsigned long long* s_acc = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(u64) * H);  // [AP][H]
+  u32* s_list = reinterpret_cast<u32*>(smem_raw + sizeof(u64) * H * (1 + AP));                   // [CAP]
   __shared__ u32 s_nused, s_n;
   __shared__ unsigned long long s_base;
   __shared__ unsigned long long s_slot_fin[Layout::kSlotted ? kServeMaxSlots * R : 1];
@@ -533,11 +542,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   unsigned long long wsum[R], fsum[R], fstates = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
-  for (int i = threadIdx.x; i < H; i += BLOCK) {
-    s_key[i] = kEmpty;
-#pragma unroll
-    for (int r = 0; r < R; ++r) s_acc[r * H + i] = 0ull;
-  }
+  for (int i = threadIdx.x; i < H; i += BLOCK) s_key[i] = kEmpty;
   if (threadIdx.x == 0) s_nused = 0;
 
   Cand<R> buf[LPT];
@@ -600,15 +605,23 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
 #pragma unroll
     for (int l = 0; l < LPT; ++l)
       if ((fresh_bits >> l) & 1u) {
+        if constexpr (kFold) {
+          s_acc[slots[l]] = crt_fold2(buf[l].res[0], buf[l].res[kFold ? 1 : 0]);
+        } else {
 #pragma unroll
-        for (int r = 0; r < R; ++r) s_acc[r * H + slots[l]] = buf[l].res[r];
+          for (int r = 0; r < R; ++r) s_acc[r * H + slots[l]] = buf[l].res[r];
+        }
       }
     __syncthreads();
 #pragma unroll
     for (int l = 0; l < LPT; ++l)
       if ((dup_bits >> l) & 1u) {
+        if constexpr (kFold) {
+          atomicAdd(&s_acc[slots[l]], (unsigned long long)crt_fold2(buf[l].res[0], buf[l].res[kFold ? 1 : 0]));
+        } else {
 #pragma unroll
-        for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slots[l]], (unsigned long long)buf[l].res[r]);
+          for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slots[l]], (unsigned long long)buf[l].res[r]);
+        }
       }
     __syncthreads();
     const u32 next = part + gridDim.x;
@@ -628,9 +641,10 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
       const u64 idx = base + i;
       const bool full = (key & L.mask_of(key)) == L.mask_of(key);
       if (write_out) keys_out[idx] = key;
+      const u64 folded = kFold ? s_acc[slot] : 0ull;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const u32 v = reduce_sum(s_acc[r * H + slot], r);
+        const u32 v = kFold ? reduce_u64(folded, r) : reduce_sum(s_acc[r * H + slot], r);
         if (write_out) res_out[r * out_stride + idx] = v;
         wsum[r] += v;
         if (full) fsum[r] += v;
@@ -709,9 +723,12 @@ template <int R, int BLOCK, int H, typename Layout>
 cudaError_t merge_shape(const PartitionCfg& pc, int blocks_per_sm, const void* regions, const u32* cursors,
                         const FrontierView& out, Layout L, bool write_out, StepScalars* sc, cudaStream_t stream) {
   if (pc.cap != (u32)(H / 2)) return cudaErrorInvalidValue;
-  auto kern = pc.merge_kind == 1 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>
-                                 : partition_merge_kernel<R, BLOCK, H, H / 2, Layout>;
-  const size_t smem = merge_smem<R, H>() + (pc.merge_kind == 1 ? (size_t)(H / 2) * 4 : 0);
+  const bool fold = R == 2 && pc.merge_kind == 1 && pc.fold;
+  auto kern = fold                 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, R == 2>
+              : pc.merge_kind == 1 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>
+                                   : partition_merge_kernel<R, BLOCK, H, H / 2, Layout>;
+  const size_t smem = fold ? merge_smem<1, H>() + (size_t)(H / 2) * 4
+                           : merge_smem<R, H>() + (pc.merge_kind == 1 ? (size_t)(H / 2) * 4 : 0);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const u64 capb = (u64)pc.sms * blocks_per_sm;

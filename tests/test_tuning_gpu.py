@@ -33,11 +33,12 @@ def tctx(qp):
     c.close()
 
 
-@pytest.mark.parametrize("scatter,ppl,merge,wide", [
-    combo for combo in itertools.product((0, 1), (2, 4), (0, 1), (0, 1))
+@pytest.mark.parametrize("scatter,ppl,merge,wide,fold", [
+    combo for combo in itertools.product((0, 1), (2, 4), (0, 1), (0, 1), (0, 1)) if combo[2] == 1 or combo[4] == 0
 ])
-def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide):
-    tctx.set_tuning(scatter_kind=scatter, parents_per_lane=ppl, merge_kind=merge, wide_merge=wide)
+def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold):
+    tctx.set_tuning(scatter_kind=scatter, parents_per_lane=ppl, merge_kind=merge, wide_merge=wide,
+                    fold_weights=fold)
     for n in (9, 13):
         got = tctx.contract_rows(n)
         want = _oracle(oracle, n)
@@ -58,7 +59,7 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 @pytest.mark.parametrize("field,value", [
     ("scatter_kind", 2), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
-    ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5),
+    ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 2),
 ])
 def test_out_of_range_tuning_is_rejected_and_kept(tctx, qp, field, value):
     before = tctx.tuning
@@ -95,3 +96,25 @@ def test_autotune_rejects_probe_sizes_outside_range(tctx, qp):
     with pytest.raises(qp.ContractionError) as e:
         tctx.autotune(n=19, repeats=1)
     assert e.value.code == qp.QPEPS_ERR_RANGE
+
+
+@pytest.mark.parametrize("n", [13, 16, 17])
+def test_folded_and_residue_accumulators_agree(tctx, qp, n):
+    tctx.set_tuning(fold_weights=0)
+    a = tctx.contract_rows(n)
+    tctx.set_tuning(fold_weights=1)
+    b = tctx.contract_rows(n)
+    assert a.count == b.count == qp.known_count(n)
+    assert _layers(a) == _layers(b)
+    assert a.device["count_residues"] == b.device["count_residues"]
+
+
+def test_fold_is_exact_at_n20_bound(tctx, qp):
+    # 20! < p0 * p1: the largest board that folds; its row weights must match
+    # the residue accumulator's on a prefix slice that runs in seconds.
+    tctx.set_tuning(fold_weights=0)
+    a = tctx.count_with_stats(20, [3, 0, 7, 11])
+    tctx.set_tuning(fold_weights=1)
+    b = tctx.count_with_stats(20, [3, 0, 7, 11])
+    assert a[0] == b[0]
+    assert a[1].device["residues"] == b[1].device["residues"] == 2
