@@ -232,13 +232,16 @@ typedef struct qpeps_serve_completion {
   qpeps_u128 count;
   int32_t status;   /* QPEPS_OK or an error code */
   uint32_t n, k;
-  uint32_t path;    /* 0 shared batch, 1 large-request context, 2 result cache, 3 host (trivial prefix) */
+  uint32_t path;    /* 0 shared batch, 1 large-request context, 2 result cache, 3 host (trivial prefix),
+                       4 waited on an identical request that was already queued or running */
   double latency_s; /* submit -> completion */
   double queue_s;   /* submit -> admission */
 } qpeps_serve_completion;
 
 typedef struct qpeps_serve_stats {
   uint64_t submitted, completed, batch_steps, cache_hits, large_runs;
+  uint64_t batch_requeued; /* requests moved from the shared batch to the large-request context */
+  uint64_t coalesced;      /* requests answered by an identical in-flight request (cache on) */
 } qpeps_serve_stats;
 
 void qpeps_serve_config_default(qpeps_serve_config* cfg);
@@ -248,6 +251,10 @@ int qpeps_serve_submit(void* server, uint32_t n, const uint32_t* prefix, uint32_
 /* Copy up to `cap` completions into `out`; waits up to `wait_ms` when none is ready. */
 int qpeps_serve_poll(void* server, qpeps_serve_completion* out, uint32_t cap, uint32_t* got, uint32_t wait_ms);
 int qpeps_serve_stats_get(void* server, qpeps_serve_stats* out);
+/* Why a server stopped: its error code and message (QPEPS_OK and "" while it
+ * runs). A request that overflows the shared batch's budget does not stop the
+ * server: the batch's requests move to the large-request context. */
+int qpeps_serve_error(void* server, char* err, size_t err_len);
 void qpeps_serve_close(void* server);
 
 /* One row step of the partitioned merge that allocates no device memory.

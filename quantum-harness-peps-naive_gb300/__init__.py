@@ -153,7 +153,9 @@ class ServeCompletion(ctypes.Structure):
 
 
 class ServeStats(ctypes.Structure):
-    _fields_ = [(f, ctypes.c_uint64) for f in ("submitted", "completed", "batch_steps", "cache_hits", "large_runs")]
+    _fields_ = [(f, ctypes.c_uint64)
+                for f in ("submitted", "completed", "batch_steps", "cache_hits", "large_runs", "batch_requeued",
+                          "coalesced")]
 
 
 class Tuning(ctypes.Structure):
@@ -218,6 +220,7 @@ _SIGNATURES = {
         [_VP, ctypes.POINTER(ServeCompletion), ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32],
     ),
     "qpeps_serve_stats_get": (ctypes.c_int, [_VP, ctypes.POINTER(ServeStats)]),
+    "qpeps_serve_error": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_size_t]),
     "qpeps_serve_close": (None, [_VP]),
     "qpeps_tuning_default": (None, [ctypes.POINTER(Tuning)]),
     "qpeps_ctx_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
@@ -522,7 +525,7 @@ def tuning_default() -> dict:
 class Server:
     """Continuous-batching counting server (qpeps_serve_*)."""
 
-    PATHS = {0: "batch", 1: "large", 2: "cache", 3: "host"}
+    PATHS = {0: "batch", 1: "large", 2: "cache", 3: "host", 4: "coalesced"}
 
     def __init__(self, device: int = 0, **cfg):
         lib = library()
@@ -553,7 +556,9 @@ class Server:
             for b in buf[: got.value]
         ]
         if rc != QPEPS_OK:
-            raise ContractionError(rc, "server stopped")
+            err = ctypes.create_string_buffer(512)
+            code = library().qpeps_serve_error(self._h, err, len(err))
+            raise ContractionError(code or rc, "server stopped: " + err.value.decode(errors="replace"))
         return out
 
     def stats(self) -> dict:

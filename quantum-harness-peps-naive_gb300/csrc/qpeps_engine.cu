@@ -1204,6 +1204,7 @@ struct ServeSlot {
   bool used = false;
   uint64_t tag = 0;
   uint32_t n = 0, k = 0;
+  std::vector<uint32_t> prefix;
   unsigned rows_left = 0;
   ServeClock::time_point t_submit, t_admit;
   std::string cache_key;
@@ -1219,6 +1220,14 @@ static std::string serve_cache_key(unsigned n, const std::vector<uint32_t>& pref
   return s;
 }
 
+// An identical request (same N and prefix, or its mirror) that arrived while
+// the first was queued or running.
+struct ServeWaiter {
+  uint64_t tag = 0;
+  uint32_t n = 0, k = 0;
+  ServeClock::time_point t_submit;
+};
+
 struct Server {
   int device = 0;
   qpeps_serve_config cfg{};
@@ -1232,8 +1241,10 @@ struct Server {
   bool stop = false;
   std::thread t_batch, t_large;
   std::map<std::string, u128> cache;
+  std::map<std::string, std::vector<ServeWaiter>> inflight;  // queued or running keys (cache on)
   qpeps_serve_stats stats{};
   std::string fatal;
+  int fatal_code = QPEPS_OK;
   // batch state (owned by the batch thread)
   ServeSlot slots[kServeMaxSlots];
   double reserved_states = 0;
@@ -1241,8 +1252,11 @@ struct Server {
   DevFrontier f;
 };
 
+// Complete a request; with `key`, also every identical request that arrived
+// while it was queued or running (they waited on it instead of running again).
 static void serve_complete(Server& sv, uint64_t tag, uint32_t n, uint32_t k, u128 count, int status, uint32_t path,
-                           ServeClock::time_point t_submit, ServeClock::time_point t_admit) {
+                           ServeClock::time_point t_submit, ServeClock::time_point t_admit,
+                           const std::string* key = nullptr) {
   const auto now = ServeClock::now();
   qpeps_serve_completion c{};
   c.tag = tag;
@@ -1257,6 +1271,23 @@ static void serve_complete(Server& sv, uint64_t tag, uint32_t n, uint32_t k, u12
     std::lock_guard<std::mutex> lk(sv.mu);
     sv.done.push_back(c);
     sv.stats.completed += 1;
+    if (key) {
+      auto it = sv.inflight.find(*key);
+      if (it != sv.inflight.end()) {
+        for (const ServeWaiter& w : it->second) {
+          qpeps_serve_completion d = c;
+          d.tag = w.tag;
+          d.n = w.n;
+          d.k = w.k;
+          d.path = 4;
+          d.latency_s = std::chrono::duration<double>(now - w.t_submit).count();
+          d.queue_s = std::max(0.0, std::chrono::duration<double>(t_admit - w.t_submit).count());
+          sv.done.push_back(d);
+          sv.stats.completed += 1;
+        }
+        sv.inflight.erase(it);
+      }
+    }
   }
   sv.cv_done.notify_all();
 }
@@ -1289,6 +1320,10 @@ static bool serve_seeds(unsigned n, const std::vector<uint32_t>& prefix, std::ve
   *row0 = (unsigned)prefix.size();
   return true;
 }
+
+// A request's frontier can exceed its estimate (centre-column prefixes carry
+// more states); admission reserves this multiple of the estimate.
+constexpr double kAdmitMargin = 2.5;
 
 static void serve_batch_loop(Server& sv) {
   Ctx& ctx = *sv.batch;
@@ -1336,28 +1371,31 @@ static void serve_batch_loop(Server& sv) {
             break;
           }
         if (free_slot < 0) break;
-        if (any && sv.reserved_states + rq.est_states > budget_states) break;
+        if (any && sv.reserved_states + kAdmitMargin * rq.est_states > budget_states) break;
         unsigned row0 = 0;
         ServeRequest r = std::move(rq);
         sv.q_small.pop_front();
         lk.unlock();
         const auto t_admit = ServeClock::now();
         if (!serve_seeds(r.n, r.prefix, seeds, &row0)) {
-          serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), 0, QPEPS_OK, 3, r.t_submit, t_admit);
+          serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), 0, QPEPS_OK, 3, r.t_submit, t_admit,
+                         &r.cache_key);
         } else if (row0 >= r.n) {
-          serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), 1, QPEPS_OK, 3, r.t_submit, t_admit);
+          serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), 1, QPEPS_OK, 3, r.t_submit, t_admit,
+                         &r.cache_key);
         } else {
           ServeSlot& sl = sv.slots[free_slot];
           sl.used = true;
           sl.tag = r.tag;
           sl.n = r.n;
           sl.k = (uint32_t)r.prefix.size();
+          sl.prefix = r.prefix;
           sl.rows_left = r.n - row0;
           sl.t_submit = r.t_submit;
           sl.t_admit = t_admit;
           sl.cache_key = r.cache_key;
-          sl.est_states = r.est_states;
-          sv.reserved_states += r.est_states;
+          sl.est_states = kAdmitMargin * r.est_states;
+          sv.reserved_states += sl.est_states;
           h_mask[free_slot] = (1ull << r.n) - 1;
           mask_dirty = true;
           for (auto& sd : seeds) {
@@ -1370,69 +1408,103 @@ static void serve_batch_loop(Server& sv) {
         lk.lock();
       }
     }
-    if (mask_dirty)
-      cuda_check(cudaMemcpyAsync(d_mask, h_mask, sizeof h_mask, cudaMemcpyHostToDevice, ctx.stream), "slot masks");
-    if (!seed_keys.empty()) {
-      // Append the seeds to the shared boundary.
-      const u64 m = seed_keys.size();
-      if (!ensure_front(ctx, p, sv.f, sv.f.count + m, ctx.table.bytes))
-        fail(QPEPS_ERR_CAPACITY, "serving batch budget cannot hold the admitted seeds");
-      char* base = static_cast<char*>(ctx.front[0].ptr);
-      cuda_check(cudaMemcpyAsync(base + sv.f.count * 8, seed_keys.data(), m * 8, cudaMemcpyHostToDevice, ctx.stream),
-                 "seed keys");
-      std::vector<uint32_t> plane(m);
-      for (int r = 0; r < 2; ++r) {
-        for (u64 i = 0; i < m; ++i) plane[i] = seed_res[2 * i + r];
-        cuda_check(cudaMemcpyAsync(base + sv.f.cap * 8 + ((size_t)r * sv.f.cap + sv.f.count) * 4, plane.data(), m * 4,
-                                   cudaMemcpyHostToDevice, ctx.stream),
-                   "seed residues");
-        cuda_check(cudaStreamSynchronize(ctx.stream), "seed upload");
-      }
-      sv.f.count += m;
-    }
-    bool active = false;
-    for (const ServeSlot& sl : sv.slots) active = active || sl.used;
-    if (!active) continue;
-    // One row for every admitted request.
-    StepScalars* sc = ctx.d_sc;
-    cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
-    FrontierView view = view_of(p, ctx.front[0], sv.f.cap);
-    cuda_check(launch_serve_count(view, sv.f.count, d_mask, sc, ctx.sms, ctx.stream), "serve count");
-    sync_scalars(ctx);
-    const u64 terms = ctx.h_sc->terms;
-    if (terms > 0) {
-      const u32 pcap = partition_capacity();
-      double mean = ctx.partition_fill * pcap;
-      for (int attempt = 0;; ++attempt) {
-        const u32 parts = (u32)std::max<u64>(1, (u64)((double)terms / mean) + 1);
-        const size_t region_bytes = (size_t)parts * pcap * candidate_bytes(2);
-        const size_t table_bytes = region_bytes + ((size_t)parts * 4 + 255) / 256 * 256;
-        if (ctx.table.bytes < table_bytes) buf_release(ctx, ctx.table);
-        if (!ensure_front(ctx, p, sv.f, std::max<u64>(sv.f.count, terms), ctx.table.ptr ? 0 : table_bytes))
-          fail(QPEPS_ERR_CAPACITY, "serving batch budget exceeded");
-        buf_reserve(ctx, ctx.table, table_bytes, p.budget, "serve partitions");
-        view = view_of(p, ctx.front[0], sv.f.cap);
-        uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
-        PartitionCfg pc{2, ctx.sms, parts, pcap, 2, 1, ctx.tune.parents_per_lane, 0, ctx.tune.scatter_kind,
-                        ctx.tune.merge_kind, ctx.tune.fold_weights};  // serving boards have N <= 19
-        cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear cursors");
-        cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
-        cuda_check(launch_serve_scatter(pc, view, sv.f.count, d_mask, ctx.table.ptr, cursors, sc, ctx.stream),
-                   "serve scatter");
-        cuda_check(launch_serve_merge(pc, ctx.table.ptr, cursors, view, d_mask, d_final, sc, ctx.stream),
-                   "serve merge");
-        sync_scalars(ctx);
-        if (ctx.h_sc->error & kErrOverflow) {
-          if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, "serving partition overflow persists");
-          mean *= 0.6;
-          continue;
+    try {
+      if (mask_dirty)
+        cuda_check(cudaMemcpyAsync(d_mask, h_mask, sizeof h_mask, cudaMemcpyHostToDevice, ctx.stream), "slot masks");
+      if (!seed_keys.empty()) {
+        // Append the seeds to the shared boundary.
+        const u64 m = seed_keys.size();
+        if (!ensure_front(ctx, p, sv.f, sv.f.count + m, ctx.table.bytes))
+          fail(QPEPS_ERR_CAPACITY, "serving batch budget cannot hold the admitted seeds");
+        char* base = static_cast<char*>(ctx.front[0].ptr);
+        cuda_check(cudaMemcpyAsync(base + sv.f.count * 8, seed_keys.data(), m * 8, cudaMemcpyHostToDevice, ctx.stream),
+                   "seed keys");
+        std::vector<uint32_t> plane(m);
+        for (int r = 0; r < 2; ++r) {
+          for (u64 i = 0; i < m; ++i) plane[i] = seed_res[2 * i + r];
+          cuda_check(cudaMemcpyAsync(base + sv.f.cap * 8 + ((size_t)r * sv.f.cap + sv.f.count) * 4, plane.data(), m * 4,
+                                     cudaMemcpyHostToDevice, ctx.stream),
+                     "seed residues");
+          cuda_check(cudaStreamSynchronize(ctx.stream), "seed upload");
         }
-        if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, "serving device capacity error");
-        break;
+        sv.f.count += m;
       }
-      sv.f.count = ctx.h_sc->out_count;
-    } else {
+      bool active = false;
+      for (const ServeSlot& sl : sv.slots) active = active || sl.used;
+      if (!active) continue;
+      // One row for every admitted request.
+      StepScalars* sc = ctx.d_sc;
+      cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
+      FrontierView view = view_of(p, ctx.front[0], sv.f.cap);
+      cuda_check(launch_serve_count(view, sv.f.count, d_mask, sc, ctx.sms, ctx.stream), "serve count");
+      sync_scalars(ctx);
+      const u64 terms = ctx.h_sc->terms;
+      if (terms > 0) {
+        const u32 pcap = partition_capacity();
+        double mean = ctx.partition_fill * pcap;
+        for (int attempt = 0;; ++attempt) {
+          const u32 parts = (u32)std::max<u64>(1, (u64)((double)terms / mean) + 1);
+          const size_t region_bytes = (size_t)parts * pcap * candidate_bytes(2);
+          const size_t table_bytes = region_bytes + ((size_t)parts * 4 + 255) / 256 * 256;
+          if (ctx.table.bytes < table_bytes) buf_release(ctx, ctx.table);
+          if (!ensure_front(ctx, p, sv.f, std::max<u64>(sv.f.count, terms), ctx.table.ptr ? 0 : table_bytes))
+            fail(QPEPS_ERR_CAPACITY, "serving batch budget exceeded");
+          buf_reserve(ctx, ctx.table, table_bytes, p.budget, "serve partitions");
+          view = view_of(p, ctx.front[0], sv.f.cap);
+          uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
+          PartitionCfg pc{2, ctx.sms, parts, pcap, 2, 1, ctx.tune.parents_per_lane, 0, ctx.tune.scatter_kind,
+                          ctx.tune.merge_kind, ctx.tune.fold_weights};  // serving boards have N <= 19
+          cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear cursors");
+          cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
+          cuda_check(launch_serve_scatter(pc, view, sv.f.count, d_mask, ctx.table.ptr, cursors, sc, ctx.stream),
+                     "serve scatter");
+          cuda_check(launch_serve_merge(pc, ctx.table.ptr, cursors, view, d_mask, d_final, sc, ctx.stream),
+                     "serve merge");
+          sync_scalars(ctx);
+          if (ctx.h_sc->error & kErrOverflow) {
+            if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, "serving partition overflow persists");
+            mean *= 0.6;
+            continue;
+          }
+          if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, "serving device capacity error");
+          break;
+        }
+        sv.f.count = ctx.h_sc->out_count;
+      } else {
+        sv.f.count = 0;
+      }
+    } catch (const Failure& e) {
+      if (e.code != QPEPS_ERR_CAPACITY) throw;
+      // The shared batch outgrew its device budget: every admitted request
+      // restarts from its prefix on the large-request context, and the batch
+      // starts empty.
+      std::vector<ServeRequest> moved;
+      for (unsigned i = 0; i < kServeMaxSlots; ++i) {
+        ServeSlot& sl = sv.slots[i];
+        if (!sl.used) continue;
+        ServeRequest r;
+        r.tag = sl.tag;
+        r.n = sl.n;
+        r.prefix = sl.prefix;
+        r.t_submit = sl.t_submit;
+        r.cache_key = sl.cache_key;
+        r.est_states = sl.est_states / kAdmitMargin;
+        moved.push_back(std::move(r));
+        sl.used = false;
+        h_mask[i] = 0;
+      }
       sv.f.count = 0;
+      buf_release(ctx, ctx.table);
+      cuda_check(cudaMemsetAsync(sv.slot_buf.ptr, 0, kServeMaxSlots * 5 * sizeof(u64), ctx.stream), "clear slots");
+      cuda_check(cudaStreamSynchronize(ctx.stream), "clear slots");
+      {
+        std::lock_guard<std::mutex> lk(sv.mu);
+        sv.reserved_states = 0;
+        sv.stats.batch_requeued += moved.size();
+        for (ServeRequest& r : moved) sv.q_large.push_back(std::move(r));
+      }
+      sv.cv.notify_all();
+      continue;
     }
     {
       std::lock_guard<std::mutex> lk(sv.mu);
@@ -1458,7 +1530,7 @@ static void serve_batch_loop(Server& sv) {
         sv.reserved_states -= sl.est_states;
         if (sv.cfg.use_cache) sv.cache[sl.cache_key] = count;
       }
-      serve_complete(sv, sl.tag, sl.n, sl.k, count, QPEPS_OK, 0, sl.t_submit, sl.t_admit);
+      serve_complete(sv, sl.tag, sl.n, sl.k, count, QPEPS_OK, 0, sl.t_submit, sl.t_admit, &sl.cache_key);
     }
   }
 }
@@ -1492,7 +1564,7 @@ static void serve_large_loop(Server& sv) {
       sv.stats.large_runs += 1;
       if (status == QPEPS_OK && sv.cfg.use_cache) sv.cache[r.cache_key] = count;
     }
-    serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), count, status, 1, r.t_submit, t_admit);
+    serve_complete(sv, r.tag, r.n, (uint32_t)r.prefix.size(), count, status, 1, r.t_submit, t_admit, &r.cache_key);
   }
 }
 
@@ -1505,6 +1577,12 @@ static void serve_thread_main(Server& sv, bool large) {
   } catch (const Failure& e) {
     std::lock_guard<std::mutex> lk(sv.mu);
     sv.fatal = e.msg;
+    sv.fatal_code = e.code;
+    sv.stop = true;
+  } catch (const std::exception& e) {
+    std::lock_guard<std::mutex> lk(sv.mu);
+    sv.fatal = e.what();
+    sv.fatal_code = QPEPS_ERR_INVALID;
     sv.stop = true;
   }
   sv.cv.notify_all();
@@ -1742,8 +1820,13 @@ int qpeps_serve_open(int device, const qpeps_serve_config* cfg, void** server_ou
       cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
       if (!sv->cfg.batch_budget_bytes) sv->cfg.batch_budget_bytes = (uint64_t)(fr * 0.25);
       if (!sv->cfg.large_budget_bytes) sv->cfg.large_budget_bytes = (uint64_t)(fr * 0.60);
+      // Requests estimated above 16 M frontier states run alone on the large
+      // context: a shared step costs as much as its largest member's row, so
+      // keeping big requests out of the batch keeps its steps (and the small
+      // requests' latency) short.
       if (!sv->cfg.large_threshold_states)
-        sv->cfg.large_threshold_states = (uint64_t)((double)sv->cfg.batch_budget_bytes / (2.4 * 16.0) / 4.0);
+        sv->cfg.large_threshold_states = std::min<uint64_t>(
+            16ull << 20, (uint64_t)((double)sv->cfg.batch_budget_bytes / (2.4 * 16.0) / 4.0));
       sv->t_batch = std::thread(serve_thread_main, std::ref(*sv), false);
       sv->t_large = std::thread(serve_thread_main, std::ref(*sv), true);
     } catch (...) {
@@ -1784,6 +1867,13 @@ int qpeps_serve_submit(void* server, uint32_t n, const uint32_t* prefix, uint32_
         serve_complete(*sv, tag, n, k, count, QPEPS_OK, 2, r.t_submit, r.t_submit);
         return;
       }
+      auto in = sv->inflight.find(r.cache_key);
+      if (in != sv->inflight.end()) {
+        in->second.push_back(ServeWaiter{tag, n, k, r.t_submit});
+        sv->stats.coalesced += 1;
+        return;
+      }
+      sv->inflight[r.cache_key];
     }
     if (r.est_states > (double)sv->cfg.large_threshold_states)
       sv->q_large.push_back(std::move(r));
@@ -1805,6 +1895,14 @@ int qpeps_serve_poll(void* server, qpeps_serve_completion* out, uint32_t cap, ui
   sv->done.erase(sv->done.begin(), sv->done.begin() + m);
   *got = m;
   return sv->fatal.empty() ? QPEPS_OK : QPEPS_ERR_CUDA;
+}
+
+int qpeps_serve_error(void* server, char* err, size_t err_len) {
+  Server* sv = static_cast<Server*>(server);
+  if (!sv) return QPEPS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  set_err(err, err_len, sv->fatal);
+  return sv->fatal.empty() ? QPEPS_OK : sv->fatal_code;
 }
 
 int qpeps_serve_stats_get(void* server, qpeps_serve_stats* out) {

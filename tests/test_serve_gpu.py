@@ -96,3 +96,44 @@ def test_trivial_prefixes(qp):
             for c in sv.poll(wait_ms=100):
                 got[c["tag"]] = c
     assert got[1]["count"] == 1 and got[2]["count"] == 0
+
+
+def test_batch_over_budget_moves_requests_to_large_context(qp, oracle):
+    # A 1 MiB shared batch cannot hold these requests' frontiers: the batch
+    # gives them to the large-request context, which finishes them exactly.
+    rng = random.Random(11)
+    reqs = [(tag, 13, qp.random_prefix(rng, 13, 1)) for tag in range(12)]
+    got = {}
+    with qp.Server(0, use_cache=0, batch_budget_bytes=1 << 20, large_threshold_states=10**12) as sv:
+        for tag, n, prefix in reqs:
+            sv.submit(n, prefix, tag)
+        deadline = time.time() + 120
+        while len(got) < len(reqs) and time.time() < deadline:
+            for c in sv.poll(wait_ms=100):
+                got[c["tag"]] = c
+        stats = sv.stats()
+    assert len(got) == len(reqs)
+    assert stats["batch_requeued"] > 0
+    for tag, n, prefix in reqs:
+        assert got[tag]["status"] == 0
+        assert got[tag]["count"] == _oracle_count(oracle, n, prefix), (n, prefix)
+
+
+def test_identical_requests_in_flight_are_coalesced(qp):
+    with qp.Server(0, use_cache=1) as sv:
+        for tag in range(6):
+            sv.submit(15, [], tag)          # identical
+        sv.submit(15, [3], 10)
+        sv.submit(15, [11], 11)             # mirror of [3]
+        got = {}
+        deadline = time.time() + 120
+        while len(got) < 8 and time.time() < deadline:
+            for c in sv.poll(wait_ms=100):
+                got[c["tag"]] = c
+        stats = sv.stats()
+    assert len(got) == 8
+    assert all(got[t]["count"] == qp.known_count(15) for t in range(6))
+    assert got[10]["count"] == got[11]["count"]
+    assert stats["coalesced"] + stats["cache_hits"] == 6
+    assert stats["coalesced"] >= 1
+    assert {got[t]["path"] for t in range(6)} - {"batch", "large", "cache", "coalesced"} == set()
