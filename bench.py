@@ -3,7 +3,11 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 18]
 
 One step = one complete exact contraction of Q(N) (all rows, all first-row
-orbit slices) through the library's C ABI. Prints one JSON line.
+orbit slices) through the library's C ABI. Prints one JSON line. By default
+the contraction runs with use_graph: the first warm-up step records its row
+steps and captures them as one CUDA graph, and every later step replays the
+whole contraction on the device from its seeds (checked row by row against the
+recorded run); --no-graph contracts eagerly every step.
 
 value  : boundary entries per second = (boundary entries of the merged
          contraction: the sum over rows of the merged frontier's input states)
@@ -15,8 +19,11 @@ value  : boundary entries per second = (boundary entries of the merged
 e2e    : the same entries / wall time of the C-ABI call (host seeding,
          host->device upload of the seed boundary, all row steps, device->host
          read-back of every row's metrics and of the count residues).
-roofline: the merge step (expand-insert + compact kernels), algorithmic bytes
-         E*(S_in+S_out) per step over the kernels' CUDA-event time.
+roofline: the merge step (scatter + merge kernels, plus the row count),
+         algorithmic bytes E*(S_in+S_out) summed over the row steps of one
+         contraction over those kernels' CUDA-event time; `traffic` is the DRAM
+         bytes ncu measured over all scatter and merge launches of one Q(18)
+         contraction with the default tuning.
 cpu_baseline: the CPU oracle (threaded restatement of the reference's
          sort-reduce driver) on the first rows of the same workload.
 
@@ -49,6 +56,9 @@ PACKAGE = "quantum-harness-peps-naive_gb300"
 # the frontier. N <= 16 match the CPU oracle; 17 and 18 were measured by this
 # library in single-batch merged runs (tail_row off, one device batch).
 MERGED_ENTRIES = {16: 397600651, 17: 2684482260, 18: 16682949222}
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) over every
+# partition scatter and merge launch of one contraction, default tuning.
+DRAM_TRAFFIC_PER_STEP = {18: 1915.5e9}
 METRIC = "Q(N) wall time & boundary entries/s at N=18 (bit-exact)"
 UNIT = "boundary entries/s"
 
@@ -190,7 +200,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     ctx = pkg.Context(local if world > 1 else 0)
-    opts = {}
+    opts = {"use_graph": 0 if args.no_graph else 1}
     if args.slice_depth:
         opts["slice_depth"] = args.slice_depth
     if args.grain == "site":
@@ -251,7 +261,8 @@ def run_ours(args):
         "peak_kind": peak_kind,
         "unit": "GB/s",
         "frac": achieved / peak,
-        "traffic": None,
+        "traffic": (DRAM_TRAFFIC_PER_STEP.get(args.n) if d["merge"] == 2 and args.grain == "row" else None),
+        "traffic_scope": "DRAM bytes per step (one contraction), ncu, all scatter + merge launches",
         "algorithmic_bytes_per_step": d["merge_kernel_bytes"],
         "launches_per_step": d["merge_kernel_launches"],
         "scatter_ms_per_step": d["scatter_kernel_ms"],
@@ -282,6 +293,7 @@ def run_ours(args):
             "merge": {1: "hash", 2: "partition"}.get(d["merge"], d["merge"]),
             "l2": "inputs larger than L2 (boundary buffers of GBs per row)",
             "parallelism": "replicas" if world > 1 else "single",
+            "cuda_graph": not args.no_graph,
         },
         "count": str(results[-1].count),
         "wall_s_per_step": wall_s,
@@ -451,6 +463,9 @@ def main():
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="contract eagerly every step (default: the first warm-up step captures the row steps "
+                         "as a CUDA graph and later steps replay it)")
     ap.add_argument("--serve", action="store_true", help="run the serving stream instead of the Q(N) step")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")

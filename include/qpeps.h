@@ -118,7 +118,10 @@ typedef struct qpeps_options {
   uint32_t symmetry;             /* 1 = first-row vertical-reflection orbits (reference default) */
   uint32_t collect_layers;       /* 1 = fill per-row metrics */
   uint32_t block_threads;        /* 0 = auto */
-  uint32_t use_graph;            /* 1 = replay row steps through captured CUDA graphs */
+  uint32_t use_graph;            /* 1 = the first contraction with these options (and tuning) on a
+                                    context records its row steps and captures them as one CUDA
+                                    graph; later identical contractions replay it (one launch, one
+                                    synchronisation) and check every row against the recorded run */
   uint64_t device_budget_bytes;  /* 0 = auto (a fraction of free device memory) */
   uint32_t tail_row;             /* rows >= tail_row run in the slice-tail kernel (a CTA contracts
                                     batches of boundary entries in shared memory); 0 = auto (never),

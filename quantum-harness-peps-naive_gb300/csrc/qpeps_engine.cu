@@ -258,6 +258,9 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+struct GraphRecorder;
+struct GraphPlan;
+
 struct Ctx {
   int device = 0;
   int sms = 0;
@@ -288,12 +291,16 @@ struct Ctx {
     double slice_margin = 2.0;                  // predictive slicing: slice peak / mean slice peak
   } tune;
   DevBuf tail;                   // TailControl + overflow list
+  uint64_t pool_gen = 0;         // bumped whenever a pool buffer is allocated or freed
+  GraphRecorder* rec = nullptr;  // row steps of the running contraction (use_graph)
+  GraphPlan* graph = nullptr;    // captured contraction (use_graph)
 };
 
 static void buf_release(Ctx& ctx, DevBuf& b) {
   if (b.ptr) {
     cudaFree(b.ptr);
     ctx.pool_bytes -= b.bytes;
+    ++ctx.pool_gen;
   }
   b.ptr = nullptr;
   b.bytes = 0;
@@ -314,11 +321,15 @@ static void buf_reserve(Ctx& ctx, DevBuf& b, size_t bytes, size_t budget, const 
   b.bytes = want;
   ctx.pool_bytes += want;
   ctx.peak_pool_bytes = std::max(ctx.peak_pool_bytes, ctx.pool_bytes);
+  ++ctx.pool_gen;
 }
+
+static void graph_free(Ctx& ctx);
 
 static void ctx_free(Ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  graph_free(*ctx);
   buf_release(*ctx, ctx->front[0]);
   buf_release(*ctx, ctx->front[1]);
   buf_release(*ctx, ctx->table);
@@ -447,6 +458,30 @@ struct StepOut {
 
 enum class StepStatus { Ok, NeedSplit };
 
+// Row steps of one contraction as launched, for CUDA-graph replay
+// (qpeps_options.use_graph): every device batch's seed and, per row step, the
+// partition configuration and the sizes the step saw.
+struct GraphStepRec {
+  PartitionCfg pc{};
+  u64 n_in = 0, terms = 0, out = 0, need_cap = 0;
+  size_t region_bytes = 0, table_bytes = 0;
+  bool final_step = false;
+  u64 weight_sum[kMaxResidues] = {0, 0, 0, 0};  // raw device sums (not reduced)
+  u64 final_sum[kMaxResidues] = {0, 0, 0, 0};
+};
+
+struct GraphChunkRec {
+  u64 count = 0;
+  std::vector<uint8_t> keys;
+  std::vector<uint32_t> res;
+  std::vector<GraphStepRec> steps;
+};
+
+struct GraphRecorder {
+  bool ok = true;  // false once anything outside the capturable form ran
+  std::vector<GraphChunkRec> chunks;
+};
+
 static size_t key_bytes(const Plan& p) { return (size_t)p.key_bits / 8; }
 
 // Grow front[0] to hold `need` entries, keeping the live ones. Returns false
@@ -469,6 +504,7 @@ static bool ensure_front(Ctx& ctx, const Plan& p, DevFrontier& f, u64 need, size
   }
   nb.bytes = want * eb;
   ctx.pool_bytes += nb.bytes;
+  ++ctx.pool_gen;
   ctx.peak_pool_bytes = std::max(ctx.peak_pool_bytes, ctx.pool_bytes);
   if (f.count) {
     const size_t kb = key_bytes(p);
@@ -511,9 +547,11 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   if (so.terms == 0) {
     f.count = 0;
     *so_out = so;
+    if (ctx.rec && !ctx.rec->chunks.empty()) ctx.rec->chunks.back().steps.push_back(GraphStepRec{});
     return StepStatus::Ok;
   }
   const bool partition = p.merge == QPEPS_MERGE_PARTITION && !site;
+  if (ctx.rec && !partition) ctx.rec->ok = false;
   const size_t eb = entry_bytes(p);
   // Wide merge CTAs halve the number of open partition tails the scatter
   // keeps in L2; they pay off once the narrow partitions no longer fit there.
@@ -605,6 +643,26 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
       so.weight[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
       so.final_sum[r] = ctx.h_sc->final_sum[r] % kPrimes[r];
     }
+    if (ctx.rec) {
+      if (ctx.rec->chunks.empty() || !partition) {
+        ctx.rec->ok = false;
+      } else {
+        GraphStepRec g;
+        g.pc = pc;
+        g.n_in = n_in;
+        g.terms = terms;
+        g.out = so.out;
+        g.need_cap = need_cap;
+        g.region_bytes = region_bytes;
+        g.table_bytes = table_bytes;
+        g.final_step = final_step;
+        for (int r = 0; r < p.R; ++r) {
+          g.weight_sum[r] = ctx.h_sc->weight_sum[r];
+          g.final_sum[r] = ctx.h_sc->final_sum[r];
+        }
+        ctx.rec->chunks.back().steps.push_back(g);
+      }
+    }
     rs.device_ms += ms_a + ms_b;
     rs.scatter_ms += ms_a;
     rs.merge_ms += ms_b;
@@ -623,6 +681,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
 // later at the same (row, site).
 static void split_to_host(Ctx& ctx, const Plan& p, DevFrontier& f, unsigned row, unsigned site, bool row_counted,
                           bool no_tail, std::vector<HostChunk>& pending) {
+  if (ctx.rec) ctx.rec->ok = false;
   const u64 keep = f.count / 2, moved = f.count - keep;
   HostChunk hc;
   hc.row = row;
@@ -667,6 +726,13 @@ static void upload_chunk(Ctx& ctx, const Plan& p, const HostChunk& hc, DevFronti
   cuda_check(cudaStreamSynchronize(ctx.stream), "upload synchronize");
   ctx.h2d_bytes += hc.count * (kb + 4u * p.R);
   f.count = hc.count;
+  if (ctx.rec) {
+    GraphChunkRec c;
+    c.count = hc.count;
+    c.keys = hc.keys;
+    c.res = hc.res;
+    ctx.rec->chunks.push_back(std::move(c));
+  }
 }
 
 static HostChunk chunk_from_items(const Plan& p, const std::vector<Item>& items, unsigned row) {
@@ -693,6 +759,7 @@ static HostChunk chunk_from_items(const Plan& p, const std::vector<Item>& items,
 // that the row engine contracts to the end.
 static void run_tail(Ctx& ctx, const Plan& p, DevFrontier& f, unsigned row0, std::vector<RowAcc>& rows, RunStats& rs,
                      std::vector<HostChunk>& pending) {
+  if (ctx.rec) ctx.rec->ok = false;
   const u64 items = f.count;
   const size_t ctl_bytes = (sizeof(TailControl) + 255) / 256 * 256;
   const size_t need = ctl_bytes + items * 8;
@@ -964,11 +1031,234 @@ static double serve_estimate(unsigned n, unsigned k) {
 static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
                           Contraction& out);
 
+// ---- CUDA-graph replay (qpeps_options.use_graph) ---------------------------
+//
+// A contraction's device work is fixed by N, the prefix, the options and the
+// tuning: the same seeds, the same per-row successor counts and the same
+// partition sizes every time. With use_graph, an eager run records its row
+// steps (GraphRecorder); if it ran as whole device batches with the
+// partitioned merge (no host spill, no tail kernel), the steps are captured
+// once into a graph: per batch a device-to-device copy of the batch's seed,
+// then per row the cursor clear, the scatter and the merge, each row's
+// scalars into its own slot, and one copy of all scalars to pinned memory at
+// the end. A later identical contraction on the same context, while the
+// context's buffers are unchanged, replays it: one graph launch and one
+// synchronisation instead of three launches and two synchronisations per row.
+// The replay checks every row's output count, weight sums and final sums
+// against the recorded run before it answers; on any difference it drops the
+// graph and contracts eagerly.
+
+struct GraphPlan {
+  unsigned n = 0;
+  std::vector<uint32_t> prefix;
+  qpeps_options opt{};
+  Ctx::Tune tune{};
+  uint64_t pool_gen = 0;
+  Contraction base;
+  std::vector<GraphChunkRec> chunks;
+  cudaGraphExec_t exec = nullptr;
+  void* seeds = nullptr;
+  StepScalars* d_scal = nullptr;
+  StepScalars* h_scal = nullptr;
+  size_t nsteps = 0;
+  uint64_t launches = 0;
+  std::vector<cudaEvent_t> ev;  // ev[0] start, then one after every kernel
+};
+
+static void graph_free(Ctx& ctx) {
+  GraphPlan* g = ctx.graph;
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->seeds) cudaFree(g->seeds);
+  if (g->d_scal) cudaFree(g->d_scal);
+  if (g->h_scal) cudaFreeHost(g->h_scal);
+  for (cudaEvent_t e : g->ev)
+    if (e) cudaEventDestroy(e);
+  delete g;
+  ctx.graph = nullptr;
+}
+
+static qpeps_options graph_key_options(const qpeps_options& o) {
+  qpeps_options k = o;
+  k.use_graph = 0;
+  k.reserved = 0;
+  return k;
+}
+
+static bool graph_matches(const Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k) {
+  const GraphPlan* g = ctx.graph;
+  if (!g || g->n != n || g->prefix.size() != k || g->pool_gen != ctx.pool_gen) return false;
+  for (unsigned i = 0; i < k; ++i)
+    if (g->prefix[i] != prefix[i]) return false;
+  const qpeps_options a = graph_key_options(o), b = graph_key_options(g->opt);
+  if (std::memcmp(&a, &b, sizeof a) != 0) return false;
+  return std::memcmp(&g->tune, &ctx.tune, sizeof g->tune) == 0;
+}
+
+// Capture the recorded steps. Best effort: any failure leaves no graph.
+static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
+                        const Contraction& done, GraphRecorder& rec) {
+  graph_free(ctx);
+  const Plan& p = done.plan;
+  if (!rec.ok || rec.chunks.empty() || p.merge != QPEPS_MERGE_PARTITION || p.grain != QPEPS_GRAIN_ROW ||
+      p.key_bits != 64 || !ctx.front[0].ptr || !ctx.table.ptr)
+    return;
+  const size_t eb = entry_bytes(p), kb = key_bytes(p);
+  const u64 cap = ctx.front[0].bytes / eb;
+  size_t seed_bytes = 0, nsteps = 0;
+  for (const GraphChunkRec& c : rec.chunks) {
+    if (c.count > cap) return;
+    seed_bytes += c.count * eb;
+    for (const GraphStepRec& st : c.steps) {
+      if (st.terms && (st.need_cap > cap || st.table_bytes > ctx.table.bytes)) return;
+      ++nsteps;
+    }
+  }
+  GraphPlan* g = new GraphPlan();
+  ctx.graph = g;
+  g->n = n;
+  g->prefix.assign(prefix, prefix + k);
+  g->opt = o;
+  g->tune = ctx.tune;
+  g->base = done;
+  g->chunks = std::move(rec.chunks);
+  g->nsteps = nsteps;
+  bool capturing = false;
+  cudaGraph_t graph = nullptr;
+  auto ok = [&](cudaError_t e) {
+    if (e != cudaSuccess) throw Failure{QPEPS_ERR_CUDA, cudaGetErrorString(e)};
+  };
+  try {
+    ok(cudaMalloc(&g->seeds, std::max<size_t>(seed_bytes, 16)));
+    ok(cudaMalloc(&g->d_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars)));
+    ok(cudaMallocHost(&g->h_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars)));
+    // Seeds: each batch's keys then its residue planes, packed.
+    size_t off = 0;
+    for (const GraphChunkRec& c : g->chunks) {
+      ok(cudaMemcpy(static_cast<char*>(g->seeds) + off, c.keys.data(), c.count * kb, cudaMemcpyHostToDevice));
+      ok(cudaMemcpy(static_cast<char*>(g->seeds) + off + c.count * kb, c.res.data(), c.count * 4u * p.R,
+                    cudaMemcpyHostToDevice));
+      off += c.count * eb;
+    }
+    ctx.h2d_bytes += seed_bytes;
+    size_t nev = 1;
+    for (const GraphChunkRec& c : g->chunks)
+      for (const GraphStepRec& st : c.steps) nev += st.terms ? 2 : 0;
+    g->ev.assign(nev, nullptr);
+    for (cudaEvent_t& e : g->ev) ok(cudaEventCreate(&e));
+
+    ok(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeRelaxed));
+    capturing = true;
+    ok(cudaMemsetAsync(g->d_scal, 0, std::max<size_t>(nsteps, 1) * sizeof(StepScalars), ctx.stream));
+    size_t ei = 0, si = 0;
+    ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
+    char* front = static_cast<char*>(ctx.front[0].ptr);
+    FrontierView view = view_of(p, ctx.front[0], cap);
+    off = 0;
+    for (const GraphChunkRec& c : g->chunks) {
+      const char* sd = static_cast<const char*>(g->seeds) + off;
+      ok(cudaMemcpyAsync(front, sd, c.count * kb, cudaMemcpyDeviceToDevice, ctx.stream));
+      for (int r = 0; r < p.R; ++r)
+        ok(cudaMemcpyAsync(front + cap * kb + (size_t)r * cap * 4, sd + c.count * kb + (size_t)r * c.count * 4,
+                           c.count * 4, cudaMemcpyDeviceToDevice, ctx.stream));
+      off += c.count * eb;
+      for (const GraphStepRec& st : c.steps) {
+        StepScalars* sc = g->d_scal + si++;
+        if (!st.terms) continue;
+        void* regions = ctx.table.ptr;
+        uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + st.region_bytes);
+        ok(cudaMemsetAsync(cursors, 0, (size_t)st.pc.parts * 4 * st.pc.cursor_stride, ctx.stream));
+        ok(launch_partition_scatter(st.pc, view, st.n_in, p.n, regions, cursors, sc, ctx.stream));
+        ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
+        ok(launch_partition_merge(st.pc, regions, cursors, view, p.n, !st.final_step, sc, ctx.stream));
+        ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
+        g->launches += 2;
+      }
+    }
+    ok(cudaMemcpyAsync(g->h_scal, g->d_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars),
+                       cudaMemcpyDeviceToHost, ctx.stream));
+    capturing = false;
+    ok(cudaStreamEndCapture(ctx.stream, &graph));
+    ok(cudaGraphInstantiate(&g->exec, graph, 0));
+    cudaGraphDestroy(graph);
+    graph = nullptr;
+    g->pool_gen = ctx.pool_gen;
+  } catch (const Failure&) {
+    if (capturing) {
+      cudaGraph_t dead = nullptr;
+      cudaStreamEndCapture(ctx.stream, &dead);
+      if (dead) cudaGraphDestroy(dead);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    graph_free(ctx);
+  }
+}
+
+// Replay the captured contraction into `out`; false when there is no matching
+// graph or the replay's scalars differ from the recorded run.
+static bool graph_replay(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
+                         Contraction& out) {
+  if (!graph_matches(ctx, n, o, prefix, k)) return false;
+  GraphPlan* g = ctx.graph;
+  const auto t0 = std::chrono::steady_clock::now();
+  cuda_check(cudaSetDevice(ctx.device), "cudaSetDevice");
+  cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+  cuda_check(cudaGraphLaunch(g->exec, ctx.stream), "graph launch");
+  cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+  cuda_check(cudaStreamSynchronize(ctx.stream), "graph synchronize");
+  ctx.d2h_bytes += std::max<size_t>(g->nsteps, 1) * sizeof(StepScalars);
+  const int R = g->base.plan.R;
+  size_t si = 0;
+  bool same = true;
+  for (const GraphChunkRec& c : g->chunks)
+    for (const GraphStepRec& st : c.steps) {
+      const StepScalars& h = g->h_scal[si++];
+      if (!st.terms) continue;
+      same = same && h.error == 0 && h.out_count == st.out;
+      for (int r = 0; r < R; ++r) same = same && h.weight_sum[r] == st.weight_sum[r] && h.final_sum[r] == st.final_sum[r];
+    }
+  if (!same) {
+    graph_free(ctx);
+    return false;
+  }
+  out = g->base;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
+  out.rs.device_ms = ms;
+  out.rs.scatter_ms = out.rs.merge_ms = 0;
+  size_t ei = 1;
+  for (const GraphChunkRec& c : g->chunks)
+    for (const GraphStepRec& st : c.steps) {
+      if (!st.terms) continue;
+      float a = 0, b = 0;
+      cudaEventElapsedTime(&a, g->ev[ei - 1], g->ev[ei]);
+      cudaEventElapsedTime(&b, g->ev[ei], g->ev[ei + 1]);
+      out.rs.scatter_ms += a;
+      out.rs.merge_ms += b;
+      ei += 2;
+    }
+  out.rs.launches = g->launches;
+  out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return true;
+}
+
 // Contraction plus the host<->device bytes it moved.
 static void contract(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
                      Contraction& out) {
   const uint64_t h0 = ctx.h2d_bytes, d0 = ctx.d2h_bytes;
-  contract_impl(ctx, n, o, prefix, k, out);
+  if (!(o.use_graph && graph_replay(ctx, n, o, prefix, k, out))) {
+    GraphRecorder rec;
+    if (o.use_graph) ctx.rec = &rec;
+    try {
+      contract_impl(ctx, n, o, prefix, k, out);
+    } catch (...) {
+      ctx.rec = nullptr;
+      throw;
+    }
+    ctx.rec = nullptr;
+    if (o.use_graph) graph_build(ctx, n, o, prefix, k, out, rec);
+  }
   out.h2d_bytes = ctx.h2d_bytes - h0;
   out.d2h_bytes = ctx.d2h_bytes - d0;
 }
