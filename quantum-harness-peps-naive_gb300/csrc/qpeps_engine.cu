@@ -1038,8 +1038,8 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
 // partition sizes every time. With use_graph, an eager run records its row
 // steps (GraphRecorder); if it ran as whole device batches with the
 // partitioned merge (no host spill, no tail kernel), the steps are captured
-// once into a graph: per batch a device-to-device copy of the batch's seed,
-// then per row the cursor clear, the scatter and the merge, each row's
+// once into a graph: per batch a copy of the batch's seed from pinned host
+// memory, then per row the cursor clear, the scatter and the merge, each row's
 // scalars into its own slot, and one copy of all scalars to pinned memory at
 // the end. A later identical contraction on the same context, while the
 // context's buffers are unchanged, replays it: one graph launch and one
@@ -1057,7 +1057,8 @@ struct GraphPlan {
   Contraction base;
   std::vector<GraphChunkRec> chunks;
   cudaGraphExec_t exec = nullptr;
-  void* seeds = nullptr;
+  void* h_seeds = nullptr;  // pinned: every batch's seed keys and residue planes, packed
+  size_t seed_bytes = 0;
   StepScalars* d_scal = nullptr;
   StepScalars* h_scal = nullptr;
   size_t nsteps = 0;
@@ -1069,7 +1070,7 @@ static void graph_free(Ctx& ctx) {
   GraphPlan* g = ctx.graph;
   if (!g) return;
   if (g->exec) cudaGraphExecDestroy(g->exec);
-  if (g->seeds) cudaFree(g->seeds);
+  if (g->h_seeds) cudaFreeHost(g->h_seeds);
   if (g->d_scal) cudaFree(g->d_scal);
   if (g->h_scal) cudaFreeHost(g->h_scal);
   for (cudaEvent_t e : g->ev)
@@ -1129,18 +1130,18 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
     if (e != cudaSuccess) throw Failure{QPEPS_ERR_CUDA, cudaGetErrorString(e)};
   };
   try {
-    ok(cudaMalloc(&g->seeds, std::max<size_t>(seed_bytes, 16)));
+    ok(cudaMallocHost(&g->h_seeds, std::max<size_t>(seed_bytes, 16)));
+    g->seed_bytes = seed_bytes;
     ok(cudaMalloc(&g->d_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars)));
     ok(cudaMallocHost(&g->h_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars)));
-    // Seeds: each batch's keys then its residue planes, packed.
+    // Seeds: each batch's keys then its residue planes, packed in pinned
+    // memory; every replay uploads them again (the graph's copy nodes).
     size_t off = 0;
     for (const GraphChunkRec& c : g->chunks) {
-      ok(cudaMemcpy(static_cast<char*>(g->seeds) + off, c.keys.data(), c.count * kb, cudaMemcpyHostToDevice));
-      ok(cudaMemcpy(static_cast<char*>(g->seeds) + off + c.count * kb, c.res.data(), c.count * 4u * p.R,
-                    cudaMemcpyHostToDevice));
+      std::memcpy(static_cast<char*>(g->h_seeds) + off, c.keys.data(), c.count * kb);
+      std::memcpy(static_cast<char*>(g->h_seeds) + off + c.count * kb, c.res.data(), c.count * 4u * p.R);
       off += c.count * eb;
     }
-    ctx.h2d_bytes += seed_bytes;
     size_t nev = 1;
     for (const GraphChunkRec& c : g->chunks)
       for (const GraphStepRec& st : c.steps) nev += st.terms ? 2 : 0;
@@ -1156,11 +1157,11 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
     FrontierView view = view_of(p, ctx.front[0], cap);
     off = 0;
     for (const GraphChunkRec& c : g->chunks) {
-      const char* sd = static_cast<const char*>(g->seeds) + off;
-      ok(cudaMemcpyAsync(front, sd, c.count * kb, cudaMemcpyDeviceToDevice, ctx.stream));
+      const char* sd = static_cast<const char*>(g->h_seeds) + off;
+      ok(cudaMemcpyAsync(front, sd, c.count * kb, cudaMemcpyHostToDevice, ctx.stream));
       for (int r = 0; r < p.R; ++r)
         ok(cudaMemcpyAsync(front + cap * kb + (size_t)r * cap * 4, sd + c.count * kb + (size_t)r * c.count * 4,
-                           c.count * 4, cudaMemcpyDeviceToDevice, ctx.stream));
+                           c.count * 4, cudaMemcpyHostToDevice, ctx.stream));
       off += c.count * eb;
       for (const GraphStepRec& st : c.steps) {
         StepScalars* sc = g->d_scal + si++;
@@ -1208,6 +1209,7 @@ static bool graph_replay(Ctx& ctx, unsigned n, const qpeps_options& o, const uin
   cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
   cuda_check(cudaStreamSynchronize(ctx.stream), "graph synchronize");
   ctx.d2h_bytes += std::max<size_t>(g->nsteps, 1) * sizeof(StepScalars);
+  ctx.h2d_bytes += g->seed_bytes;
   const int R = g->base.plan.R;
   size_t si = 0;
   bool same = true;
