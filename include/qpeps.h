@@ -176,6 +176,34 @@ int qpeps_count_batch(void* ctx, uint32_t num, const uint32_t* n, const uint32_t
  * own C. */
 int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len);
 
+/* ---- Explicit-C generic site frontier -------------------------------------
+ * Replaces contract_explicit_c_frontier (src/lib.rs:961-967, kernel
+ * 1519-1711): contract the explicit C tensor one site at a time in row-major
+ * or top-left-diamond order; the boundary is the values of the open virtual
+ * bonds (u128 keys). N > 21 -> QPEPS_ERR_RANGE; support_limit = 0 ->
+ * QPEPS_ERR_INVALID. When a site's merged boundary exceeds support_limit the
+ * result is incomplete (complete = 0, count unset, contracted_sites = the
+ * sites finished before it, peak_states = support_limit + 1); its tensor
+ * counters then cover the whole failing site, where the reference's stop
+ * inside it. */
+#define QPEPS_ORDER_ROW_MAJOR 0
+#define QPEPS_ORDER_TOP_LEFT_DIAMOND 1
+
+typedef struct qpeps_explicit_result {
+  uint32_t n, order, complete, pad0;
+  qpeps_u128 count;
+  double elapsed_s;
+  uint64_t peak_states, peak_open_bonds;
+  qpeps_u128 tensor_entries_examined, tensor_entries_accepted;
+  uint64_t contracted_sites;
+  uint64_t peak_rss_bytes; /* device memory high-water mark of the context */
+  uint64_t gpu_launches;
+  double device_ms;
+} qpeps_explicit_result;
+
+int qpeps_explicit_frontier(void* ctx, uint32_t n, uint32_t order, uint64_t support_limit,
+                            qpeps_explicit_result* out, char* err, size_t err_len);
+
 /* ---- Tuning ---------------------------------------------------------------
  * No reference counterpart (the reference has one CPU code path): the knobs of
  * the partitioned merge, held per context. Every setting gives the same

@@ -75,6 +75,26 @@ def build() -> Path:
     return LIB
 
 
+class OqExplicit(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint32),
+        ("order", ctypes.c_uint32),
+        ("complete", ctypes.c_uint32),
+        ("pad", ctypes.c_uint32),
+        ("count", OqU128),
+        ("elapsed_s", ctypes.c_double),
+        ("peak_states", ctypes.c_uint64),
+        ("peak_open_bonds", ctypes.c_uint64),
+        ("tensor_entries_examined", OqU128),
+        ("tensor_entries_accepted", OqU128),
+        ("contracted_sites", ctypes.c_uint64),
+    ]
+
+
+ROW_MAJOR = 0  # ExplicitFrontierOrder::RowMajor (src/lib.rs:940-944)
+TOP_LEFT_DIAMOND = 1  # ExplicitFrontierOrder::TopLeftDiamond
+
+
 def lib() -> ctypes.CDLL:
     global _lib
     with _lock:
@@ -111,6 +131,8 @@ def lib() -> ctypes.CDLL:
             L.oracle_unpack.restype = None
             L.oracle_row_terms.argtypes = [ctypes.c_uint32, ctypes.c_int, OqU128, P(OqU128), P(OqU128), ctypes.c_uint32]
             L.oracle_orbit_weight.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+            L.oracle_explicit_frontier.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, P(OqExplicit),
+                                                   ctypes.c_char_p, ctypes.c_size_t]
             _lib = L
         return _lib
 
@@ -275,3 +297,24 @@ def row_terms(n: int, parent_key: int, sitewise: bool):
 
 def orbit_weight(n: int, column: int) -> int:
     return lib().oracle_orbit_weight(n, column)
+
+
+def explicit_frontier(n: int, order: int = ROW_MAJOR, support_limit: int = 5_000_000) -> dict:
+    """contract_explicit_c_frontier (src/lib.rs:961-967) restated; returns a
+    dict shaped like ExplicitFrontierResult (count None when incomplete)."""
+    out = OqExplicit()
+    err = ctypes.create_string_buffer(512)
+    if lib().oracle_explicit_frontier(n, order, support_limit, ctypes.byref(out), err, len(err)):
+        raise OracleError(err.value.decode())
+    return {
+        "n": out.n,
+        "order": out.order,
+        "complete": bool(out.complete),
+        "count": out.count.value if out.complete else None,
+        "elapsed": out.elapsed_s,
+        "peak_states": out.peak_states,
+        "peak_open_bonds": out.peak_open_bonds,
+        "tensor_entries_examined": out.tensor_entries_examined.value,
+        "tensor_entries_accepted": out.tensor_entries_accepted.value,
+        "contracted_sites": out.contracted_sites,
+    }

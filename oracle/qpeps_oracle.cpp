@@ -701,6 +701,183 @@ static ContractionResult contract_rows_with_backend(unsigned n, bool sitewise, c
 }
 
 // known_count, src/lib.rs:5752-5784 (OEIS A000170, Q(0..27)).
+// ---------------------------------------------------------------------------
+// Explicit-C generic site frontier (src/lib.rs:940-967, 1419-1711): contract
+// the explicit C tensor one site at a time over an arbitrary site order, the
+// boundary being the values of the currently open virtual bonds (bit i of a
+// key = value of the i-th open bond in increasing bond id).
+
+// A site leg: a virtual bond shared with a neighbouring site, or an open
+// boundary leg whose allowed values are the set bits of `allowed`
+// (FrontierLeg, src/lib.rs:1419-1491).
+struct OqFrontierLeg {
+  bool edge;
+  unsigned id;
+  u8 allowed;
+};
+
+struct OqFrontierSite {
+  unsigned row, column;
+  OqFrontierLeg legs[8];  // column in/out, row in/out, dr in/out, dl in/out
+};
+
+// explicit_frontier_sites, src/lib.rs:1419-1491: bond ids of the four bond
+// families (row bonds, column bonds, down-right and down-left diagonal
+// bonds); edge-of-board legs are open: incoming legs carry 0, outgoing column
+// and row legs must carry 1 (one queen per column / row), outgoing diagonal
+// legs are free.
+static std::vector<OqFrontierSite> explicit_frontier_sites(unsigned n) {
+  const unsigned span = n ? n - 1 : 0;
+  const unsigned column_base = n * span, dr_base = column_base + n * span, dl_base = dr_base + span * span;
+  auto bond = [](unsigned id) { return OqFrontierLeg{true, id, 0}; };
+  auto open = [](u8 allowed) { return OqFrontierLeg{false, 0, allowed}; };
+  std::vector<OqFrontierSite> sites;
+  sites.reserve((size_t)n * n);
+  for (unsigned r = 0; r < n; ++r)
+    for (unsigned c = 0; c < n; ++c) {
+      OqFrontierSite s{r, c, {}};
+      s.legs[0] = r == 0 ? open(0b01) : bond(column_base + (r - 1) * n + c);
+      s.legs[1] = r + 1 == n ? open(0b10) : bond(column_base + r * n + c);
+      s.legs[2] = c == 0 ? open(0b01) : bond(r * span + c - 1);
+      s.legs[3] = c + 1 == n ? open(0b10) : bond(r * span + c);
+      s.legs[4] = (r == 0 || c == 0) ? open(0b01) : bond(dr_base + (r - 1) * span + c - 1);
+      s.legs[5] = (r + 1 == n || c + 1 == n) ? open(0b11) : bond(dr_base + r * span + c);
+      s.legs[6] = (r == 0 || c + 1 == n) ? open(0b01) : bond(dl_base + (r - 1) * span + c);
+      s.legs[7] = (r + 1 == n || c == 0) ? open(0b11) : bond(dl_base + r * span + c - 1);
+      sites.push_back(s);
+    }
+  return sites;
+}
+
+// explicit_frontier_order, src/lib.rs:1493-1503: row-major, or by
+// (row + column, row) for the top-left diamond.
+static std::vector<unsigned> explicit_frontier_order(unsigned n, unsigned order) {
+  std::vector<unsigned> idx((size_t)n * n);
+  for (unsigned i = 0; i < idx.size(); ++i) idx[i] = i;
+  if (order == 1)
+    std::sort(idx.begin(), idx.end(), [n](unsigned a, unsigned b) {
+      const unsigned ra = a / n, rb = b / n, sa = ra + a % n, sb = rb + b % n;
+      return sa != sb ? sa < sb : ra < rb;
+    });
+  return idx;
+}
+
+struct ExplicitFrontierResult {
+  unsigned n = 0, order = 0;
+  bool complete = false;
+  u128 count = 0;
+  double elapsed = 0;
+  u64 peak_states = 1, peak_open_bonds = 0;
+  u128 examined = 0, accepted = 0;
+  u64 contracted_sites = 0;
+};
+
+// contract_explicit_c_frontier_kernel, src/lib.rs:1519-1711.
+static ExplicitFrontierResult contract_explicit_c_frontier(unsigned n, unsigned order, u64 support_limit) {
+  if (n > 21) throw Error{"explicit-C frontier key supports N <= 21"};
+  if (support_limit == 0) throw Error{"explicit-C frontier support limit must be positive"};
+  ExplicitFrontierResult res;
+  res.n = n;
+  res.order = order;
+  if (n == 0) {
+    res.complete = true;
+    res.count = 1;
+    return res;
+  }
+  const SiteTensorC tensor = SiteTensorC::sec_vi();
+  if (tensor.entries.size() != 17) throw Error{"explicit-C frontier requires the Sec. VI 17-entry tensor"};
+  const auto sites = explicit_frontier_sites(n);
+  const auto ordering = explicit_frontier_order(n, order);
+  std::unordered_map<u128, u128, U128Hash> boundary{{0, 1}};
+  std::vector<unsigned> open_edges;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (size_t step = 0; step < ordering.size(); ++step) {
+    const OqFrontierSite& site = sites[ordering[step]];
+    std::unordered_map<unsigned, unsigned> old_pos;
+    for (unsigned i = 0; i < open_edges.size(); ++i) old_pos[open_edges[i]] = i;
+    std::vector<unsigned> incident;
+    for (const OqFrontierLeg& l : site.legs)
+      if (l.edge) incident.push_back(l.id);
+    std::vector<unsigned> next;
+    for (unsigned e : open_edges)
+      if (std::find(incident.begin(), incident.end(), e) == incident.end()) next.push_back(e);
+    for (unsigned e : incident)
+      if (!old_pos.count(e)) next.push_back(e);
+    std::sort(next.begin(), next.end());
+    if (next.size() > 128)
+      throw Error{"explicit-C frontier exceeds 128 open bonds at site (" + std::to_string(site.row) + "," +
+                  std::to_string(site.column) + ")"};
+    std::unordered_map<unsigned, unsigned> next_pos;
+    for (unsigned i = 0; i < next.size(); ++i) next_pos[next[i]] = i;
+    std::vector<std::pair<unsigned, unsigned>> carry;  // (old position, next position)
+    for (unsigned i = 0; i < open_edges.size(); ++i) {
+      auto it = next_pos.find(open_edges[i]);
+      if (it != next_pos.end()) carry.push_back({i, it->second});
+    }
+    struct Transition {
+      u128 required_mask, required_value, added_value, local_value;
+    };
+    std::vector<Transition> transitions;
+    for (const CEntry& e : tensor.entries) {
+      const u8 values[8] = {e.legs.column_in,  e.legs.column_out,  e.legs.row_in,     e.legs.row_out,
+                            e.legs.diag_dr_in, e.legs.diag_dr_out, e.legs.diag_dl_in, e.legs.diag_dl_out};
+      Transition t{0, 0, 0, e.value};
+      bool keep = true;
+      for (int l = 0; l < 8 && keep; ++l) {
+        const OqFrontierLeg& leg = site.legs[l];
+        if (!leg.edge) {
+          keep = (leg.allowed >> values[l]) & 1;
+        } else {
+          auto it = old_pos.find(leg.id);
+          if (it != old_pos.end()) {
+            t.required_mask |= (u128)1 << it->second;
+            t.required_value |= (u128)values[l] << it->second;
+          } else {
+            t.added_value |= (u128)values[l] << next_pos[leg.id];
+          }
+        }
+      }
+      if (keep) transitions.push_back(t);
+    }
+    std::unordered_map<u128, u128, U128Hash> candidates;
+    for (const auto& kv : boundary) {
+      res.examined += 17;
+      u128 carried = 0;
+      for (const auto& cp : carry) carried |= ((kv.first >> cp.first) & 1) << cp.second;
+      for (const Transition& t : transitions) {
+        if ((kv.first & t.required_mask) != t.required_value) continue;
+        res.accepted += 1;
+        u128 contribution;
+        if (!checked_mul(kv.second, t.local_value, &contribution))
+          throw Error{"explicit-C coefficient multiplication overflow at site (" + std::to_string(site.row) + "," +
+                      std::to_string(site.column) + ")"};
+        u128& acc = candidates[carried | t.added_value];
+        if (!checked_add(acc, contribution, &acc))
+          throw Error{"explicit-C coefficient addition overflow at site (" + std::to_string(site.row) + "," +
+                      std::to_string(site.column) + ")"};
+        if (candidates.size() > support_limit) {
+          res.peak_states = std::max<u64>(res.peak_states, candidates.size());
+          res.peak_open_bonds = std::max<u64>(res.peak_open_bonds, next.size());
+          res.contracted_sites = step;
+          res.elapsed = seconds_since(t0);
+          return res;
+        }
+      }
+    }
+    boundary.swap(candidates);
+    open_edges.swap(next);
+    res.peak_states = std::max<u64>(res.peak_states, boundary.size());
+    res.peak_open_bonds = std::max<u64>(res.peak_open_bonds, open_edges.size());
+  }
+  if (!open_edges.empty()) throw Error{"explicit-C contraction ended with uncontracted virtual bonds"};
+  auto it = boundary.find(0);
+  res.count = it == boundary.end() ? 0 : it->second;
+  res.complete = true;
+  res.contracted_sites = (u64)n * n;
+  res.elapsed = seconds_since(t0);
+  return res;
+}
+
 static bool known_count(unsigned n, u128* out) {
   static const char* counts[28] = {"1",
                                    "1",
@@ -1233,6 +1410,38 @@ int oracle_row_terms(uint32_t n, int mode, oq_u128 parent, oq_u128* keys_out, oq
 
 int oracle_orbit_weight(uint32_t n, uint32_t column) {
   return (int)top_row_vertical_orbit_weight(n, BoundaryState{(u64)1 << column, 0, 0});
+}
+
+typedef struct {
+  uint32_t n, order, complete, pad;
+  oq_u128 count;
+  double elapsed_s;
+  uint64_t peak_states, peak_open_bonds;
+  oq_u128 tensor_entries_examined, tensor_entries_accepted;
+  uint64_t contracted_sites;
+} oq_explicit;
+
+int oracle_explicit_frontier(uint32_t n, uint32_t order, uint64_t support_limit, oq_explicit* out, char* err,
+                             size_t err_len) {
+  try {
+    if (order > 1) throw Error{"order must be 0 (row-major) or 1 (top-left diamond)"};
+    const ExplicitFrontierResult r = contract_explicit_c_frontier(n, order, support_limit);
+    out->n = r.n;
+    out->order = r.order;
+    out->complete = r.complete;
+    out->pad = 0;
+    out->count = to_oq(r.count);
+    out->elapsed_s = r.elapsed;
+    out->peak_states = r.peak_states;
+    out->peak_open_bonds = r.peak_open_bonds;
+    out->tensor_entries_examined = to_oq(r.examined);
+    out->tensor_entries_accepted = to_oq(r.accepted);
+    out->contracted_sites = r.contracted_sites;
+    return 0;
+  } catch (const Error& e) {
+    set_err(err, err_len, e.msg);
+    return 1;
+  }
 }
 
 }  // extern "C"

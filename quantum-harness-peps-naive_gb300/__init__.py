@@ -158,6 +158,29 @@ class ServeStats(ctypes.Structure):
                           "coalesced")]
 
 
+ORDER_ROW_MAJOR = 0
+ORDER_TOP_LEFT_DIAMOND = 1
+
+
+class ExplicitResult(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint32),
+        ("order", ctypes.c_uint32),
+        ("complete", ctypes.c_uint32),
+        ("pad0", ctypes.c_uint32),
+        ("count", U128),
+        ("elapsed_s", ctypes.c_double),
+        ("peak_states", ctypes.c_uint64),
+        ("peak_open_bonds", ctypes.c_uint64),
+        ("tensor_entries_examined", U128),
+        ("tensor_entries_accepted", U128),
+        ("contracted_sites", ctypes.c_uint64),
+        ("peak_rss_bytes", ctypes.c_uint64),
+        ("gpu_launches", ctypes.c_uint64),
+        ("device_ms", ctypes.c_double),
+    ]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [
         ("struct_size", ctypes.c_uint32),
@@ -222,6 +245,11 @@ _SIGNATURES = {
     "qpeps_serve_stats_get": (ctypes.c_int, [_VP, ctypes.POINTER(ServeStats)]),
     "qpeps_serve_error": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_size_t]),
     "qpeps_serve_close": (None, [_VP]),
+    "qpeps_explicit_frontier": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ExplicitResult), ctypes.c_char_p,
+         ctypes.c_size_t],
+    ),
     "qpeps_tuning_default": (None, [ctypes.POINTER(Tuning)]),
     "qpeps_ctx_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "qpeps_ctx_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning), ctypes.c_char_p, ctypes.c_size_t]),
@@ -452,6 +480,31 @@ class Context:
         _check(rc, err)
         return [counts[i].value for i in range(num)]
 
+
+    def explicit_frontier(self, n: int, order: int = ORDER_ROW_MAJOR, support_limit: int = 5_000_000) -> dict:
+        """Replaces ``contract_explicit_c_frontier(n, order, support_limit)``
+        (src/lib.rs:961-967); ``count`` is None when the result is incomplete."""
+        out = ExplicitResult()
+        err = ctypes.create_string_buffer(512)
+        with self._lock:
+            rc = library().qpeps_explicit_frontier(self._h, int(n), int(order), int(support_limit), ctypes.byref(out),
+                                                   err, len(err))
+        _check(rc, err)
+        return {
+            "n": out.n,
+            "order": out.order,
+            "complete": bool(out.complete),
+            "count": out.count.value if out.complete else None,
+            "elapsed": out.elapsed_s,
+            "peak_states": out.peak_states,
+            "peak_open_bonds": out.peak_open_bonds,
+            "tensor_entries_examined": out.tensor_entries_examined.value,
+            "tensor_entries_accepted": out.tensor_entries_accepted.value,
+            "contracted_sites": out.contracted_sites,
+            "peak_rss_bytes": out.peak_rss_bytes,
+            "gpu_launches": out.gpu_launches,
+            "device_ms": out.device_ms,
+        }
 
     # ---- tuning (no reference counterpart) ---------------------------------
     @property

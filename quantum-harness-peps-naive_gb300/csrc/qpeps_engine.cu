@@ -1031,6 +1031,230 @@ static double serve_estimate(unsigned n, unsigned k) {
 static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const uint32_t* prefix, unsigned k,
                           Contraction& out);
 
+// ---- Explicit-C generic site frontier (src/lib.rs:940-967, 1419-1711) ------
+//
+// Each site has eight legs (column, row, down-right and down-left diagonal,
+// in and out). A leg is a virtual bond shared with the neighbouring site, or
+// an open board-edge leg with its allowed values: incoming legs carry 0,
+// outgoing column and row legs must carry 1 (one queen per column and row),
+// outgoing diagonals are free. Bond ids follow the reference's numbering
+// (row bonds, column bonds, down-right, down-left), so the sorted open-bond
+// list and with it every key bit position and the counters match its run.
+
+struct FrontierLegH {
+  bool bond;
+  unsigned id;
+  uint8_t allowed;  // open leg: bit v set = value v allowed
+};
+
+struct FrontierSiteH {
+  unsigned row, column;
+  FrontierLegH legs[8];  // column in/out, row in/out, dr in/out, dl in/out
+};
+
+static std::vector<FrontierSiteH> frontier_sites(unsigned n) {
+  const unsigned span = n - 1, col0 = n * span, dr0 = col0 + n * span, dl0 = dr0 + span * span;
+  auto b = [](unsigned id) { return FrontierLegH{true, id, 0}; };
+  auto e = [](uint8_t allowed) { return FrontierLegH{false, 0, allowed}; };
+  std::vector<FrontierSiteH> out;
+  for (unsigned r = 0; r < n; ++r)
+    for (unsigned c = 0; c < n; ++c) {
+      FrontierSiteH st{r, c, {}};
+      const bool top = r == 0, bottom = r + 1 == n, left = c == 0, right = c + 1 == n;
+      st.legs[0] = top ? e(1) : b(col0 + (r - 1) * n + c);
+      st.legs[1] = bottom ? e(2) : b(col0 + r * n + c);
+      st.legs[2] = left ? e(1) : b(r * span + c - 1);
+      st.legs[3] = right ? e(2) : b(r * span + c);
+      st.legs[4] = (top || left) ? e(1) : b(dr0 + (r - 1) * span + c - 1);
+      st.legs[5] = (bottom || right) ? e(3) : b(dr0 + r * span + c);
+      st.legs[6] = (top || right) ? e(1) : b(dl0 + (r - 1) * span + c);
+      st.legs[7] = (bottom || left) ? e(3) : b(dl0 + r * span + c - 1);
+      out.push_back(st);
+    }
+  return out;
+}
+
+struct ExplicitRun {
+  unsigned n = 0, order = 0;
+  bool complete = false;
+  u128 count = 0;
+  double elapsed = 0, device_ms = 0;
+  u64 peak_states = 1, peak_open_bonds = 0, contracted_sites = 0, launches = 0;
+  u128 examined = 0, accepted = 0;
+};
+
+static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_limit, ExplicitRun& out) {
+  const auto t0 = std::chrono::steady_clock::now();
+  if (n > 21) fail(QPEPS_ERR_RANGE, "explicit-C frontier key supports N <= 21");
+  if (support_limit == 0) fail(QPEPS_ERR_INVALID, "explicit-C frontier support limit must be positive");
+  if (order > 1) fail(QPEPS_ERR_INVALID, "order must be QPEPS_ORDER_ROW_MAJOR or QPEPS_ORDER_TOP_LEFT_DIAMOND");
+  out = ExplicitRun{};
+  out.n = n;
+  out.order = order;
+  if (n == 0) {
+    out.complete = true;
+    out.count = 1;
+    return;
+  }
+  certify_c(ctx.c);
+  if (ctx.c.size() != 17) fail(QPEPS_ERR_INVALID, "explicit-C frontier requires the Sec. VI 17-entry tensor");
+  cuda_check(cudaSetDevice(ctx.device), "cudaSetDevice");
+  const std::vector<FrontierSiteH> sites = frontier_sites(n);
+  std::vector<unsigned> ordering((size_t)n * n);
+  for (unsigned i = 0; i < ordering.size(); ++i) ordering[i] = i;
+  if (order == QPEPS_ORDER_TOP_LEFT_DIAMOND)
+    std::stable_sort(ordering.begin(), ordering.end(), [n](unsigned a, unsigned b) {
+      const unsigned da = a / n + a % n, db = b / n + b % n;
+      return da != db ? da < db : a / n < b / n;
+    });
+
+  Plan p{};
+  p.n = n;
+  p.R = crt_plan(n);
+  p.key_bits = 128;
+  p.grain = QPEPS_GRAIN_SITE;
+  p.merge = QPEPS_MERGE_HASH;
+  {
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    p.budget = (size_t)((double)(fr + ctx.pool_bytes) * 0.90);
+  }
+  p.threads = 256;
+  p.tail_row = n;
+  const size_t eb = entry_bytes(p);
+  DevFrontier f;
+  buf_release(ctx, ctx.front[1]);
+  f.cap = ctx.front[0].ptr ? ctx.front[0].bytes / eb : 0;
+  if (!ensure_front(ctx, p, f, 1024, 0)) fail(QPEPS_ERR_CAPACITY, "device budget cannot hold the seed boundary");
+  {
+    // Seed: the empty boundary (key 0) with weight 1.
+    char* base = static_cast<char*>(ctx.front[0].ptr);
+    cuda_check(cudaMemsetAsync(base, 0, 16, ctx.stream), "seed key");
+    const uint32_t one = 1;
+    for (int r = 0; r < p.R; ++r)
+      cuda_check(cudaMemcpyAsync(base + f.cap * 16 + (size_t)r * f.cap * 4, &one, 4, cudaMemcpyHostToDevice,
+                                 ctx.stream),
+                 "seed weight");
+    cuda_check(cudaStreamSynchronize(ctx.stream), "seed");
+    ctx.h2d_bytes += 4u * p.R;
+    f.count = 1;
+  }
+  LaunchCfg cfg{128, p.R, 256, ctx.sms};
+  std::vector<unsigned> open;
+  u64 weight_res[kMaxResidues] = {0, 0, 0, 0};
+  for (size_t step = 0; step < ordering.size(); ++step) {
+    const FrontierSiteH& site = sites[ordering[step]];
+    auto pos_in = [](const std::vector<unsigned>& v, unsigned id) -> int {
+      auto it = std::lower_bound(v.begin(), v.end(), id);
+      return (it != v.end() && *it == id) ? (int)(it - v.begin()) : -1;
+    };
+    std::vector<unsigned> incident;
+    for (const FrontierLegH& l : site.legs)
+      if (l.bond) incident.push_back(l.id);
+    std::vector<unsigned> next;
+    for (unsigned id : open)
+      if (std::find(incident.begin(), incident.end(), id) == incident.end()) next.push_back(id);
+    for (unsigned id : incident)
+      if (pos_in(open, id) < 0) next.push_back(id);
+    std::sort(next.begin(), next.end());
+    if (next.size() > 128) {
+      char buf[96];
+      std::snprintf(buf, sizeof buf, "explicit-C frontier exceeds 128 open bonds at site (%u,%u)", site.row,
+                    site.column);
+      fail(QPEPS_ERR_RANGE, buf);
+    }
+    // Bonds that stay open keep their order: group them into runs that move
+    // by one shift each.
+    FrontierStepDev st;
+    std::memset(&st, 0, sizeof st);
+    int prev_old = -2, prev_new = -2;
+    for (unsigned i = 0; i < open.size(); ++i) {
+      const int j = pos_in(next, open[i]);
+      if (j < 0) continue;
+      if ((int)i == prev_old + 1 && j == prev_new + 1 && st.n_runs > 0) {
+        st.run_mask[st.n_runs - 1] |= (u128)1 << i;
+      } else {
+        if (st.n_runs == (uint32_t)kFrontierMaxRuns) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier: too many bond runs");
+        st.run_mask[st.n_runs] = (u128)1 << i;
+        st.run_shift[st.n_runs] = j - (int)i;
+        ++st.n_runs;
+      }
+      prev_old = (int)i;
+      prev_new = j;
+    }
+    for (const CEntryH& e : ctx.c) {
+      const Legs lg = legs_from_key(e.legs);
+      const uint8_t values[8] = {lg.ci, lg.co, lg.ri, lg.ro, lg.dri, lg.dro, lg.dli, lg.dlo};
+      u128 req_mask = 0, req_value = 0, added = 0;
+      bool keep = true;
+      for (int l = 0; l < 8 && keep; ++l) {
+        const FrontierLegH& leg = site.legs[l];
+        if (!leg.bond) {
+          keep = (leg.allowed >> values[l]) & 1;
+        } else if (const int i = pos_in(open, leg.id); i >= 0) {
+          req_mask |= (u128)1 << i;
+          req_value |= (u128)values[l] << i;
+        } else {
+          added |= (u128)values[l] << pos_in(next, leg.id);
+        }
+      }
+      if (!keep) continue;
+      st.req_mask[st.n_trans] = req_mask;
+      st.req_value[st.n_trans] = req_value;
+      st.added[st.n_trans] = added;
+      ++st.n_trans;
+    }
+    out.examined += (u128)f.count * 17;
+    // Every incoming leg of a site is a bond of an earlier site or a board
+    // edge in both orders, so at most two C entries match a key.
+    const u64 need = std::max<u64>(f.count * 2, 1);
+    const u64 slots = pow2_at_least(std::max<u64>(1024, need * 2));
+    const size_t table_bytes = slots * slot_bytes(128, p.R);
+    if (ctx.table.bytes < table_bytes) buf_release(ctx, ctx.table);
+    if (!ensure_front(ctx, p, f, need, ctx.table.ptr ? 0 : table_bytes))
+      fail(QPEPS_ERR_CAPACITY, "device budget exceeded by the explicit-C frontier");
+    buf_reserve(ctx, ctx.table, table_bytes, p.budget, "explicit-C frontier table");
+    FrontierView view = view_of(p, ctx.front[0], f.cap);
+    cuda_check(upload_frontier_step(st, ctx.stream), "frontier step");
+    cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
+    cuda_check(cudaMemsetAsync(ctx.table.ptr, 0, table_bytes, ctx.stream), "clear table");
+    cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+    cuda_check(launch_frontier_expand_insert(cfg, view, f.count, ctx.table.ptr, slots, ctx.d_sc, ctx.stream),
+               "frontier expand-insert kernel");
+    cuda_check(launch_compact(cfg, ctx.table.ptr, slots, view, 0, true, ctx.d_sc, ctx.stream), "compact kernel");
+    cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+    out.launches += 2;
+    sync_scalars(ctx);
+    if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier table probe bound exceeded");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
+    out.device_ms += ms;
+    out.accepted += ctx.h_sc->terms;
+    const u64 merged = ctx.h_sc->out_count;
+    if (merged > support_limit) {
+      out.peak_states = std::max<u64>(out.peak_states, support_limit + 1);
+      out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next.size());
+      out.contracted_sites = step;
+      out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return;
+    }
+    f.count = merged;
+    for (int r = 0; r < p.R; ++r) weight_res[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
+    open.swap(next);
+    out.peak_states = std::max<u64>(out.peak_states, merged);
+    out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, open.size());
+  }
+  if (!open.empty()) fail(QPEPS_ERR_INVALID, "explicit-C contraction ended with uncontracted virtual bonds");
+  // No bond is open: the boundary is the single key 0 (or empty) and its
+  // weight is the count.
+  if (f.count > 1) fail(QPEPS_ERR_INVALID, "explicit-C contraction ended with more than one closed boundary");
+  out.count = f.count ? crt_reconstruct(weight_res, p.R) : 0;
+  if (out.count > factorial(n)) fail(QPEPS_ERR_CRT_BOUND, "CRT reconstruction exceeds certified N! count bound");
+  out.complete = true;
+  out.contracted_sites = (u64)n * n;
+  out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 // ---- CUDA-graph replay (qpeps_options.use_graph) ---------------------------
 //
 // A contraction's device work is fixed by N, the prefix, the options and the
@@ -2077,6 +2301,30 @@ int qpeps_ctx_device_name(void* ctx, char* out, size_t len) {
   if (cudaGetDeviceProperties(&prop, static_cast<Ctx*>(ctx)->device) != cudaSuccess) return QPEPS_ERR_CUDA;
   std::snprintf(out, len, "%s", prop.name);
   return QPEPS_OK;
+}
+
+int qpeps_explicit_frontier(void* ctx, uint32_t n, uint32_t order, uint64_t support_limit,
+                            qpeps_explicit_result* out, char* err, size_t err_len) {
+  return guarded(err, err_len, [&] {
+    if (!ctx || !out) fail(QPEPS_ERR_INVALID, "null context or result");
+    Ctx& c = *static_cast<Ctx*>(ctx);
+    ExplicitRun r;
+    explicit_frontier(c, n, order, support_limit, r);
+    std::memset(out, 0, sizeof *out);
+    out->n = r.n;
+    out->order = r.order;
+    out->complete = r.complete ? 1 : 0;
+    out->count = to_abi(r.complete ? r.count : 0);
+    out->elapsed_s = r.elapsed;
+    out->peak_states = r.peak_states;
+    out->peak_open_bonds = r.peak_open_bonds;
+    out->tensor_entries_examined = to_abi(r.examined);
+    out->tensor_entries_accepted = to_abi(r.accepted);
+    out->contracted_sites = r.contracted_sites;
+    out->peak_rss_bytes = c.peak_pool_bytes;
+    out->gpu_launches = r.launches;
+    out->device_ms = r.device_ms;
+  });
 }
 
 int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, char* err, size_t err_len) {

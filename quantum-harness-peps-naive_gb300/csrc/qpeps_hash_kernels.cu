@@ -19,6 +19,7 @@
 namespace qpeps {
 
 __constant__ CTableDev c_table;
+__constant__ FrontierStepDev c_frontier;
 
 static_assert(sizeof(Slot<u64, 1>) == 16 && sizeof(Slot<u64, 2>) == 32 && sizeof(Slot<u64, 3>) == 32 &&
                   sizeof(Slot<u64, 4>) == 64,
@@ -413,6 +414,78 @@ cudaError_t launch_compact(const LaunchCfg& cfg, const void* table, uint64_t tab
         reinterpret_cast<const Slot<K, R>*>(table), table_slots, out.keys, out.res, out.cap, n, write_out ? 1 : 0, sc);
     return cudaGetLastError();
   });
+}
+
+// ---------------------------------------------------------------------------
+// Explicit-C generic site frontier (src/lib.rs:1519-1711): one site step.
+
+namespace {
+
+__device__ __forceinline__ u128 shift_u128(u128 v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
+
+template <int R, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) frontier_expand_insert_kernel(const u128* __restrict__ keys,
+                                                                       const u32* __restrict__ res, u64 res_stride,
+                                                                       u64 n_in, Slot<u128, R>* __restrict__ table,
+                                                                       u64 mask, StepScalars* __restrict__ sc) {
+  unsigned long long accepted = 0;
+  bool failed = false;  // probe bound hit (error already flagged): stop inserting, still reach the block sum
+  const u32 n_runs = c_frontier.n_runs, n_trans = c_frontier.n_trans;
+  for (u64 i = (u64)blockIdx.x * BLOCK + threadIdx.x; i < n_in && !failed; i += (u64)gridDim.x * BLOCK) {
+    const u128 key = keys[i];
+    u128 moved = 0;
+    for (u32 r = 0; r < n_runs; ++r) moved |= shift_u128(key & c_frontier.run_mask[r], c_frontier.run_shift[r]);
+    u32 w[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) w[r] = res[r * res_stride + i];
+    for (u32 t = 0; t < n_trans; ++t) {
+      if ((key & c_frontier.req_mask[t]) != c_frontier.req_value[t]) continue;
+      ++accepted;
+      if (!table_insert<u128, R>(table, mask, moved | c_frontier.added[t], w, kMaxProbe, &sc->error)) {
+        failed = true;
+        break;
+      }
+    }
+  }
+  const unsigned long long t = block_sum_u64<BLOCK>(accepted);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->terms, t);
+}
+
+}  // namespace
+
+cudaError_t upload_frontier_step(const FrontierStepDev& step, cudaStream_t stream) {
+  return cudaMemcpyToSymbolAsync(c_frontier, &step, sizeof step, 0, cudaMemcpyHostToDevice, stream);
+}
+
+cudaError_t launch_frontier_expand_insert(const LaunchCfg& cfg, const FrontierView& in, uint64_t n_in, void* table,
+                                          uint64_t table_slots, StepScalars* sc, cudaStream_t stream) {
+  if (n_in == 0) return cudaSuccess;
+  if (cfg.key_bits != 128 || (table_slots & (table_slots - 1))) return cudaErrorInvalidValue;
+  constexpr int kBlock = 256;
+  const u64 want = (n_in + kBlock - 1) / kBlock;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(want, (u64)cfg.sms * 8));
+  const u128* keys = reinterpret_cast<const u128*>(in.keys);
+  switch (cfg.residues) {
+    case 1:
+      frontier_expand_insert_kernel<1, kBlock><<<grid, kBlock, 0, stream>>>(
+          keys, in.res, in.cap, n_in, reinterpret_cast<Slot<u128, 1>*>(table), table_slots - 1, sc);
+      break;
+    case 2:
+      frontier_expand_insert_kernel<2, kBlock><<<grid, kBlock, 0, stream>>>(
+          keys, in.res, in.cap, n_in, reinterpret_cast<Slot<u128, 2>*>(table), table_slots - 1, sc);
+      break;
+    case 3:
+      frontier_expand_insert_kernel<3, kBlock><<<grid, kBlock, 0, stream>>>(
+          keys, in.res, in.cap, n_in, reinterpret_cast<Slot<u128, 3>*>(table), table_slots - 1, sc);
+      break;
+    case 4:
+      frontier_expand_insert_kernel<4, kBlock><<<grid, kBlock, 0, stream>>>(
+          keys, in.res, in.cap, n_in, reinterpret_cast<Slot<u128, 4>*>(table), table_slots - 1, sc);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace qpeps

@@ -71,6 +71,28 @@ cudaError_t launch_compact(const LaunchCfg& cfg, const void* table, uint64_t tab
 // Bytes per table slot for a key width / residue count.
 size_t slot_bytes(int key_bits, int residues);
 
+// Explicit-C generic site frontier: one site step. The boundary key holds the
+// values of the open virtual bonds (bit i = i-th open bond in increasing bond
+// id). The bonds that stay open move to their new positions by a few masked
+// shifts (the map is monotone), and every C entry allowed at the site becomes
+// a transition: a key matching (req_mask, req_value) on the bonds the site
+// closes yields the moved key OR `added` (the values of the bonds it opens).
+constexpr int kFrontierMaxRuns = 16;
+constexpr int kFrontierMaxTrans = 17;
+struct FrontierStepDev {
+  uint32_t n_runs, n_trans;
+  int32_t run_shift[kFrontierMaxRuns];  // > 0 left, < 0 right
+  unsigned __int128 run_mask[kFrontierMaxRuns];
+  unsigned __int128 req_mask[kFrontierMaxTrans], req_value[kFrontierMaxTrans], added[kFrontierMaxTrans];
+};
+
+cudaError_t upload_frontier_step(const FrontierStepDev& step, cudaStream_t stream);
+
+// Every (boundary entry, matching transition) successor into the u128-keyed
+// global table; `scalars->terms` receives the number of matches.
+cudaError_t launch_frontier_expand_insert(const LaunchCfg& cfg, const FrontierView& in, uint64_t n_in, void* table,
+                                          uint64_t table_slots, StepScalars* scalars, cudaStream_t stream);
+
 // Partitioned merge (u64 keys): `parts` hash partitions of `cap` candidate
 // slots each.
 struct PartitionCfg {

@@ -13,6 +13,9 @@ contraction path (nothing is computed here):
 * dense per-row layers at N=14 (sitewise)  benchmarks/n14_layers.csv
 * naive dense HashMap N=14..16 peak        benchmarks/issue34_same_node_algorithm_comparison_scnet.csv
 * CRT known answers                        src/lib.rs:3767, 6530-6545; benchmarks/scnet_e50_scaling_n1_n19_release.csv
+* explicit-C generic frontier (row-major and top-left diamond site orders):
+  count, peak support, peak open bonds, tensor entries examined/accepted,
+  contracted sites for N=7..12                benchmarks/e34_corner_frontier_release.csv
 """
 from __future__ import annotations
 
@@ -86,6 +89,16 @@ def main(ref: Path) -> None:
                 residues = [int(x) for x in row[14].split("|")]
                 crt_n19 = {"count": int(row[3]), "primes": primes, "residues": residues}
 
+    explicit = {}
+    with open(bench / "e34_corner_frontier_release.csv") as f:
+        for row in csv.DictReader(f):
+            explicit.setdefault(row["order"], {})[row["N"]] = {
+                k: int(row[k])
+                for k in ("count", "peak_support", "peak_open_bonds", "tensor_entries_examined",
+                          "tensor_entries_accepted", "contracted_sites", "total_sites", "support_limit")
+            }
+            explicit[row["order"]][row["N"]]["complete"] = row["complete"] == "true"
+
     golden = {
         "source": "EricNie2003/quantum-harness-peps-naive (reference tree), values copied from files listed in make_golden.py",
         "known_count": [str(v) for v in known],
@@ -95,6 +108,7 @@ def main(ref: Path) -> None:
         "e36_orbit_n16": e36,
         "n14_dense_sitewise_layers": n14,
         "naive_dense_hashmap": naive,
+        "explicit_frontier": explicit,
         "crt": {
             "candidate_primes": crt_primes,
             "kat_value_q27": str(crt_kat_value),

@@ -20,6 +20,7 @@ STRUCTS = {
     "qpeps_serve_completion": "ServeCompletion",
     "qpeps_serve_stats": "ServeStats",
     "qpeps_tuning": "Tuning",
+    "qpeps_explicit_result": "ExplicitResult",
 }
 
 

@@ -288,3 +288,42 @@ def test_prefix_sum_rule(oracle):
         total2 = sum(oracle.contract(n, symmetry=False, prefix=p)["count"]
                      for p in itertools.product(range(n), repeat=2))
         assert total2 == oracle.known_count(n)
+
+
+# ---- explicit-C generic site frontier (src/lib.rs:1419-1711) -----------------
+
+ORDERS = {"RowMajor": 0, "TopLeftDiamond": 1}
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_explicit_frontier_small_boards_match_known_counts(oracle, golden, order):
+    # generic_explicit_c_frontiers_match_known_counts, src/lib.rs:6123-6136
+    for n in range(0, 7):
+        r = oracle.explicit_frontier(n, order, 5_000_000)
+        assert r["complete"]
+        assert r["count"] == int(golden["known_count"][n])
+        assert r["contracted_sites"] == n * n
+
+
+@pytest.mark.parametrize("order_name", ["RowMajor", "TopLeftDiamond"])
+@pytest.mark.parametrize("n", [7, 8, 9, 10, 11])
+def test_explicit_frontier_matches_published_counters(oracle, golden, order_name, n):
+    want = golden["explicit_frontier"][order_name][str(n)]
+    r = oracle.explicit_frontier(n, ORDERS[order_name], want["support_limit"])
+    assert r["complete"] == want["complete"]
+    assert r["count"] == want["count"]
+    assert r["peak_states"] == want["peak_support"]
+    assert r["peak_open_bonds"] == want["peak_open_bonds"]
+    assert r["tensor_entries_examined"] == want["tensor_entries_examined"]
+    assert r["tensor_entries_accepted"] == want["tensor_entries_accepted"]
+    assert r["contracted_sites"] == want["contracted_sites"] == want["total_sites"]
+
+
+def test_explicit_frontier_support_limit_and_range_errors(oracle):
+    r = oracle.explicit_frontier(8, 0, 100)
+    assert not r["complete"] and r["count"] is None
+    assert r["peak_states"] == 101 and 0 < r["contracted_sites"] < 64
+    with pytest.raises(oracle.OracleError, match="N <= 21"):
+        oracle.explicit_frontier(22, 0, 10)
+    with pytest.raises(oracle.OracleError, match="support limit must be positive"):
+        oracle.explicit_frontier(5, 0, 0)
