@@ -398,6 +398,7 @@ struct RunStats {
 
 struct Plan {
   unsigned n;
+  unsigned free_rows;  // rows after the placed prefix: the count and every row weight are at most free_rows!
   int R;
   int key_bits;
   int grain;
@@ -598,7 +599,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
     PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane,
                     wide, ctx.tune.scatter_kind, ctx.tune.merge_kind,
-                    (ctx.tune.fold_weights && p.R == 2 && p.n <= 20) ? 1u : 0u};
+                    (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
     void* regions = ctx.table.ptr;
     uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
     if (partition)
@@ -947,13 +948,14 @@ struct Contraction {
   double elapsed = 0;
 };
 
-static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o) {
+static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned free_rows) {
   Plan p;
   p.n = n;
   p.grain = o.granularity == QPEPS_GRAIN_SITE ? QPEPS_GRAIN_SITE : QPEPS_GRAIN_ROW;
-  p.R = o.residues ? (int)o.residues : crt_plan(n);
+  p.free_rows = free_rows;
+  p.R = o.residues ? (int)o.residues : crt_plan(free_rows);
   if (p.R < 1 || p.R > kMaxResidues) fail(QPEPS_ERR_INVALID, "residue count must be in 1..=4");
-  if (o.residues && p.R < crt_plan(n))
+  if (o.residues && p.R < crt_plan(free_rows))
     fail(QPEPS_ERR_RANGE, "forced residue count does not certify N! for this N");
   const unsigned narrow_max = p.grain == QPEPS_GRAIN_SITE ? 20 : 21;
   if (o.key_bits == 0)
@@ -1110,6 +1112,7 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
 
   Plan p{};
   p.n = n;
+  p.free_rows = n;
   p.R = crt_plan(n);
   p.key_bits = 128;
   p.grain = QPEPS_GRAIN_SITE;
@@ -1505,7 +1508,9 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
     cuda_check(upload_c_table(ctx.c_dev, ctx.stream), "upload C table");
     ctx.c_uploaded = true;
   }
-  out.plan = make_plan(ctx, n, o);
+  // Completions of a k-row prefix place n - k queens in distinct columns:
+  // the count and every row weight are at most (n - k)!.
+  out.plan = make_plan(ctx, n, o, n - std::min(k, n));
   const u64 mask = (1ull << n) - 1;
   std::vector<Item> items;
   unsigned row0 = 0;
@@ -1582,7 +1587,8 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
   u64 res[kMaxResidues];
   for (int r = 0; r < out.plan.R; ++r) res[r] = out.rs.final_res[r];
   out.count = crt_reconstruct(res, out.plan.R);
-  if (out.count > factorial(n)) fail(QPEPS_ERR_CRT_BOUND, "CRT reconstruction exceeds certified N! count bound");
+  if (out.count > factorial(out.plan.free_rows))
+    fail(QPEPS_ERR_CRT_BOUND, "CRT reconstruction exceeds certified N! count bound");
   out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -1846,6 +1852,7 @@ static void serve_batch_loop(Server& sv) {
   cuda_check(cudaSetDevice(sv.device), "cudaSetDevice");
   Plan p{};
   p.n = 19;
+  p.free_rows = 19;
   p.R = 2;
   p.key_bits = 64;
   p.grain = QPEPS_GRAIN_ROW;

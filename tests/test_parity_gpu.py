@@ -8,6 +8,7 @@ published golden values.
 """
 from __future__ import annotations
 
+import math
 import random
 
 import pytest
@@ -98,6 +99,44 @@ def test_forced_wide_keys_are_exact(ctx, oracle, n):
     assert _gpu_layers(g) == _oracle_layers(o)
     s = ctx.contract_rows(n, key_bits=128, granularity=1)
     assert s.count == o["count"]
+
+
+def _legal_prefix(n, k, seed):
+    import random
+
+    rng = random.Random(seed)
+    while True:
+        cols, ok = [], True
+        for r in range(k):
+            free = [c for c in range(n) if all(c != q and abs(c - q) != r - i for i, q in enumerate(cols))]
+            if not free:
+                ok = False
+                break
+            cols.append(rng.choice(free))
+        if ok:
+            return cols
+
+
+@pytest.mark.parametrize("n,k", [(22, 7), (24, 9), (26, 11), (28, 13), (30, 15), (42, 30)])
+def test_boards_beyond_u64_keys_use_u128_keys_and_match_oracle(ctx, oracle, n, k):
+    # N >= 22: the packed boundary needs 3N > 64 bits, so keys are u128 and
+    # the merge is the global table (natural, not forced); N = 42 is the
+    # widest board the reference accepts. The
+    # prefixes keep the oracle's frontier at up to about 0.4 M states.
+    prefix = _legal_prefix(n, k, 1000 + n)
+    count, res = ctx.count_with_stats(n, prefix)
+    assert res.device["key_bits"] == 128
+    # residues certify (N - k)!: completions place N - k queens in distinct columns
+    bound, prod, want_r = math.factorial(n - k), 1, 0
+    for p in (2147483647, 2147483629, 2147483587, 2147483579):
+        prod *= p
+        want_r += 1
+        if prod > bound:
+            break
+    assert res.device["residues"] == want_r
+    want = oracle.contract(n, backend=oracle.PARALLEL_SORT_REDUCE, threads=8, symmetry=False, prefix=prefix)
+    assert count == want["count"]
+    assert res.peak_states == want["peak_states"]
 
 
 @pytest.mark.parametrize("residues", [1, 2, 3, 4])
