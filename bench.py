@@ -150,6 +150,17 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(values, device="cpu"):
+    """Element-wise maximum of per-rank timings over the process group (the
+    slowest replica sets the step time)."""
+    import torch  # noqa: PLC0415
+    import torch.distributed as dist  # noqa: PLC0415
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -238,12 +249,7 @@ def run_ours(args):
     dev_s = max(sum(x.device["device_ms"] for x in results) / len(results) / 1e3, 1e-12)
     wall_s = max(t_all / args.steps, 1e-12)
     if world > 1:
-        import torch  # noqa: PLC0415
-        import torch.distributed as dist  # noqa: PLC0415
-
-        t = torch.tensor([dev_s, wall_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall_s = float(t[0]), float(t[1])
+        dev_s, wall_s = max_over_ranks([dev_s, wall_s], device="cuda")
     if rank != 0:
         return
     value = entries * world / dev_s
