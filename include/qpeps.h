@@ -221,8 +221,10 @@ typedef struct qpeps_tuning {
   uint32_t wide_merge;           /* 0 never, 1 always, 2 auto: 8192-slot merge CTAs, 4096-candidate partitions */
   uint32_t wide_above_parts;     /* auto: 2048-candidate partition count above which merges go wide */
   uint32_t spread_cursors_below; /* partition counts up to which cursors get 32-byte spacing */
-  uint32_t fold_weights;         /* 1 = claim-list merge keeps one 64-bit CRT-folded value per key
-                                    instead of two residue sums (used only where N! < p0 * p1) */
+  uint32_t fold_weights;         /* claim-list merge accumulator where weights fit (two residues,
+                                    N - k <= 20): 0 = two residue sums, 1 = one 64-bit CRT-folded
+                                    value per key, 2 = the boundary carries exact 64-bit weights
+                                    (default; the row merge only, else 1) */
   double partition_fill;         /* mean candidates per partition / capacity, in [0.3, 0.95] */
   double slice_margin;           /* predictive slicing: assumed slice peak / mean slice peak, >= 1 */
 } qpeps_tuning;

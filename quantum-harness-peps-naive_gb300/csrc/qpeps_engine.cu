@@ -286,7 +286,8 @@ struct Ctx {
     uint32_t wide_above_parts = 524288;         // 2048-candidate partitions beyond which auto goes wide
     uint32_t scatter_kind = 1;                  // PartitionCfg::scatter_kind
     uint32_t merge_kind = 1;                    // PartitionCfg::merge_kind
-    uint32_t fold_weights = 1;                  // PartitionCfg::fold where exact (R = 2, N <= 20)
+    uint32_t fold_weights = 2;                  // 0 residues, 1 CRT fold, 2 exact 64-bit weights in the
+                                                // boundary (modes 1-2 only where exact: R = 2, N - k <= 20)
     double partition_fill = 0.83;               // starting value of Ctx::partition_fill
     double slice_margin = 2.0;                  // predictive slicing: slice peak / mean slice peak
   } tune;
@@ -406,6 +407,7 @@ struct Plan {
   size_t budget;
   int threads;
   unsigned tail_row;  // rows >= tail_row go to the slice-tail kernel (n = none)
+  bool w64 = false;   // residue planes 0/1 hold the low/high words of exact weights (partitioned row merge)
 };
 
 static size_t entry_bytes(const Plan& p) { return (size_t)(p.key_bits / 8) + 4u * p.R; }
@@ -599,7 +601,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
     PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane,
                     wide, ctx.tune.scatter_kind, ctx.tune.merge_kind,
-                    (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
+                    p.w64 ? 2u : (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
     void* regions = ctx.table.ptr;
     uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
     if (partition)
@@ -641,8 +643,9 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     cudaEventElapsedTime(&ms_b, ctx.ev[1], ctx.ev[2]);
     so.out = ctx.h_sc->out_count;
     for (int r = 0; r < p.R; ++r) {
-      so.weight[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
-      so.final_sum[r] = ctx.h_sc->final_sum[r] % kPrimes[r];
+      // Exact weights: plane 0 carries the exact sums.
+      so.weight[r] = ctx.h_sc->weight_sum[p.w64 ? 0 : r] % kPrimes[r];
+      so.final_sum[r] = ctx.h_sc->final_sum[p.w64 ? 0 : r] % kPrimes[r];
     }
     if (ctx.rec) {
       if (ctx.rec->chunks.empty() || !partition) {
@@ -750,7 +753,12 @@ static HostChunk chunk_from_items(const Plan& p, const std::vector<Item>& items,
     } else {
       std::memcpy(&hc.keys[i * 16], &items[i].key, 16);
     }
-    for (int r = 0; r < p.R; ++r) hc.res[(size_t)r * hc.count + i] = (uint32_t)(items[i].weight % kPrimes[r]);
+    if (p.w64) {
+      hc.res[i] = (uint32_t)items[i].weight;
+      hc.res[hc.count + i] = (uint32_t)(items[i].weight >> 32);
+    } else {
+      for (int r = 0; r < p.R; ++r) hc.res[(size_t)r * hc.count + i] = (uint32_t)(items[i].weight % kPrimes[r]);
+    }
   }
   return hc;
 }
@@ -988,6 +996,10 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
     p.tail_row = n;  // auto: the merged row engine for every row (fastest measured through N=18)
   else
     p.tail_row = (tail_ok && o.tail_row < n) ? o.tail_row : n;
+  // Exact 64-bit weights: every weight and row sum is at most free_rows!
+  // (<= 20! < 2^63) and only the partitioned row merge reads the planes.
+  p.w64 = ctx.tune.fold_weights == 2 && ctx.tune.merge_kind == 1 && p.R == 2 && p.free_rows <= 20 &&
+          p.merge == QPEPS_MERGE_PARTITION && p.grain == QPEPS_GRAIN_ROW && p.key_bits == 64 && p.tail_row >= n;
   return p;
 }
 
@@ -1976,7 +1988,7 @@ static void serve_batch_loop(Server& sv) {
           view = view_of(p, ctx.front[0], sv.f.cap);
           uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
           PartitionCfg pc{2, ctx.sms, parts, pcap, 2, 1, ctx.tune.parents_per_lane, 0, ctx.tune.scatter_kind,
-                          ctx.tune.merge_kind, ctx.tune.fold_weights};  // serving boards have N <= 19
+                          ctx.tune.merge_kind, ctx.tune.fold_weights ? 1u : 0u};  // serving: N <= 19
           cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4, ctx.stream), "clear cursors");
           cuda_check(cudaMemsetAsync(sc, 0, sizeof(StepScalars), ctx.stream), "clear scalars");
           cuda_check(launch_serve_scatter(pc, view, sv.f.count, d_mask, ctx.table.ptr, cursors, sc, ctx.stream),
@@ -2139,7 +2151,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
-  if (q.fold_weights > 1) fail(QPEPS_ERR_INVALID, "fold_weights must be 0 or 1");
+  if (q.fold_weights > 2) fail(QPEPS_ERR_INVALID, "fold_weights must be 0, 1 or 2");
   if (!(q.partition_fill >= 0.3 && q.partition_fill <= 0.95))
     fail(QPEPS_ERR_INVALID, "partition_fill must be in [0.3, 0.95]");
   if (!(q.slice_margin >= 1.0 && q.slice_margin <= 64.0)) fail(QPEPS_ERR_INVALID, "slice_margin must be in [1, 64]");

@@ -110,8 +110,9 @@ struct PartitionCfg {
                                   // 1 = per-warp shared-memory candidate window
   uint32_t merge_kind = 1;        // merge: 0 = ballot/scan compaction over the whole table,
                                   // 1 = claim list + first-claimant stores (three phases)
-  uint32_t fold = 0;              // merge_kind 1, R = 2: accumulate the CRT-folded value in one
-                                  // 64-bit plane (exact only when N! < p0 * p1, i.e. N <= 20)
+  uint32_t fold = 0;              // merge_kind 1, R = 2, one 64-bit accumulator plane:
+                                  // 1 = CRT-folded residues, 2 = the planes hold an exact weight's
+                                  // low and high words (both exact only when N! < p0 * p1, N <= 20)
 };
 
 size_t candidate_bytes(int residues);

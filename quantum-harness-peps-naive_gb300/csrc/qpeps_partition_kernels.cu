@@ -509,13 +509,28 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
 // enters the table. Same inputs, outputs and sums as partition_merge_kernel;
 // the order of the written entries differs.
 //
-// kFold (R = 2): a candidate's residue pair is folded into the one value
-// below p0 * p1 it stands for (crt_fold2) and keys accumulate that value in a
-// single 64-bit plane. This is exact when every weight and every sum of
+// kAcc selects the accumulator (R = 2 for modes 1 and 2):
+//   0: R residue planes, summed per plane and reduced on output;
+//   1: a candidate's residue pair is folded into the one value below p0 * p1
+//      it stands for (crt_fold2), accumulated in a single 64-bit plane and
+//      reduced back to residues on output;
+//   2: the two planes hold the low and high words of the exact weight, which
+//      is accumulated in a single 64-bit plane and written back as words.
+// Modes 1 and 2 are exact when every weight and every sum of weights stays
+// below p0 * p1 (about 4.6e18) and 2^63; the engine uses them for N <= 20. This is exact when every weight and every sum of
 // weights stays below p0 * p1 (about 4.6e18) and 2^64: a row's weights sum to
 // at most the number of partial placements, at most N! (20! = 2.4e18), so the
 // engine folds for N <= 20.
-template <int R, int BLOCK, int H, int CAP, typename Layout, bool kFold = false>
+// The one-plane accumulator value of a candidate's two u32 words.
+template <int kAcc>
+__device__ __forceinline__ u64 one_plane(u32 w0, u32 w1) {
+  if constexpr (kAcc == 2)
+    return (u64)w0 | ((u64)w1 << 32);
+  else
+    return crt_fold2(w0, w1);
+}
+
+template <int R, int BLOCK, int H, int CAP, typename Layout, int kAcc = 0>
 __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<R>* __restrict__ regions,
                                                                      const u32* __restrict__ cursors, u32 cstride,
                                                                      u32 parts, u64* __restrict__ keys_out,
@@ -526,7 +541,9 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   constexpr int kLogH = 31 - __builtin_clz(H);
   constexpr int LPT = CAP / BLOCK;  // candidate loads per thread
   static_assert(CAP % BLOCK == 0, "shape");
-  static_assert(!kFold || R == 2, "the folded accumulator holds one residue pair");
+  constexpr bool kFold = kAcc != 0;  // one 64-bit accumulator plane
+  static_assert(!kFold || R == 2, "the one-plane accumulators hold a residue pair or a weight's two words");
+  static_assert(kAcc != 2 || !Layout::kSlotted, "exact weights are not used by the serving layout");
   constexpr int AP = kFold ? 1 : R;  // accumulator planes
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* s_key = reinterpret_cast<u64*>(smem_raw);
@@ -606,7 +623,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     for (int l = 0; l < LPT; ++l)
       if ((fresh_bits >> l) & 1u) {
         if constexpr (kFold) {
-          s_acc[slots[l]] = crt_fold2(buf[l].res[0], buf[l].res[kFold ? 1 : 0]);
+          s_acc[slots[l]] = one_plane<kAcc>(buf[l].res[0], buf[l].res[kFold ? 1 : 0]);
         } else {
 #pragma unroll
           for (int r = 0; r < R; ++r) s_acc[r * H + slots[l]] = buf[l].res[r];
@@ -617,7 +634,8 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     for (int l = 0; l < LPT; ++l)
       if ((dup_bits >> l) & 1u) {
         if constexpr (kFold) {
-          atomicAdd(&s_acc[slots[l]], (unsigned long long)crt_fold2(buf[l].res[0], buf[l].res[kFold ? 1 : 0]));
+          atomicAdd(&s_acc[slots[l]],
+                    (unsigned long long)one_plane<kAcc>(buf[l].res[0], buf[l].res[kFold ? 1 : 0]));
         } else {
 #pragma unroll
           for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slots[l]], (unsigned long long)buf[l].res[r]);
@@ -642,12 +660,21 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
       const bool full = (key & L.mask_of(key)) == L.mask_of(key);
       if (write_out) keys_out[idx] = key;
       const u64 folded = kFold ? s_acc[slot] : 0ull;
+      if constexpr (kAcc == 2) {
+        if (write_out) {
+          res_out[idx] = (u32)folded;
+          res_out[out_stride + idx] = (u32)(folded >> 32);
+        }
+        wsum[0] += folded;
+        if (full) fsum[0] += folded;
+      } else {
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const u32 v = kFold ? reduce_u64(folded, r) : reduce_sum(s_acc[r * H + slot], r);
-        if (write_out) res_out[r * out_stride + idx] = v;
-        wsum[r] += v;
-        if (full) fsum[r] += v;
+        for (int r = 0; r < R; ++r) {
+          const u32 v = kFold ? reduce_u64(folded, r) : reduce_sum(s_acc[r * H + slot], r);
+          if (write_out) res_out[r * out_stride + idx] = v;
+          wsum[r] += v;
+          if (full) fsum[r] += v;
+        }
       }
       s_key[slot] = kEmpty;
       fstates += full;
@@ -724,9 +751,14 @@ cudaError_t merge_shape(const PartitionCfg& pc, int blocks_per_sm, const void* r
                         const FrontierView& out, Layout L, bool write_out, StepScalars* sc, cudaStream_t stream) {
   if (pc.cap != (u32)(H / 2)) return cudaErrorInvalidValue;
   const bool fold = R == 2 && pc.merge_kind == 1 && pc.fold;
-  auto kern = fold                 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, R == 2>
-              : pc.merge_kind == 1 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>
-                                   : partition_merge_kernel<R, BLOCK, H, H / 2, Layout>;
+  const bool exact = fold && pc.fold == 2;
+  if (pc.fold == 2 && !exact) return cudaErrorInvalidValue;  // exact words need the claim-list merge
+  if constexpr (Layout::kSlotted)
+    if (exact) return cudaErrorInvalidValue;
+  auto kern = fold ? (exact ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, (R == 2 && !Layout::kSlotted) ? 2 : 0>
+                            : partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, R == 2 ? 1 : 0>)
+                   : pc.merge_kind == 1 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>
+                                        : partition_merge_kernel<R, BLOCK, H, H / 2, Layout>;
   const size_t smem = fold ? merge_smem<1, H>() + (size_t)(H / 2) * 4
                            : merge_smem<R, H>() + (pc.merge_kind == 1 ? (size_t)(H / 2) * 4 : 0);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

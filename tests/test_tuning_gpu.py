@@ -34,7 +34,7 @@ def tctx(qp):
 
 
 @pytest.mark.parametrize("scatter,ppl,merge,wide,fold", [
-    combo for combo in itertools.product((0, 1), (2, 4), (0, 1), (0, 1), (0, 1)) if combo[2] == 1 or combo[4] == 0
+    combo for combo in itertools.product((0, 1), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
 ])
 def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold):
     tctx.set_tuning(scatter_kind=scatter, parents_per_lane=ppl, merge_kind=merge, wide_merge=wide,
@@ -59,7 +59,7 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 @pytest.mark.parametrize("field,value", [
     ("scatter_kind", 2), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
-    ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 2),
+    ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 3),
 ])
 def test_out_of_range_tuning_is_rejected_and_kept(tctx, qp, field, value):
     before = tctx.tuning
@@ -99,22 +99,36 @@ def test_autotune_rejects_probe_sizes_outside_range(tctx, qp):
 
 
 @pytest.mark.parametrize("n", [13, 16, 17])
-def test_folded_and_residue_accumulators_agree(tctx, qp, n):
-    tctx.set_tuning(fold_weights=0)
-    a = tctx.contract_rows(n)
-    tctx.set_tuning(fold_weights=1)
-    b = tctx.contract_rows(n)
-    assert a.count == b.count == qp.known_count(n)
-    assert _layers(a) == _layers(b)
-    assert a.device["count_residues"] == b.device["count_residues"]
+def test_folded_exact_and_residue_accumulators_agree(tctx, qp, n):
+    runs = []
+    for fold in (0, 1, 2):
+        tctx.set_tuning(fold_weights=fold)
+        runs.append(tctx.contract_rows(n))
+    assert all(r.count == qp.known_count(n) for r in runs)
+    assert _layers(runs[0]) == _layers(runs[1]) == _layers(runs[2])
+    assert runs[0].device["count_residues"] == runs[1].device["count_residues"] == runs[2].device["count_residues"]
 
 
-def test_fold_is_exact_at_n20_bound(tctx, qp):
-    # 20! < p0 * p1: the largest board that folds; its row weights must match
-    # the residue accumulator's on a prefix slice that runs in seconds.
-    tctx.set_tuning(fold_weights=0)
-    a = tctx.count_with_stats(20, [3, 0, 7, 11])
-    tctx.set_tuning(fold_weights=1)
-    b = tctx.count_with_stats(20, [3, 0, 7, 11])
-    assert a[0] == b[0]
-    assert a[1].device["residues"] == b[1].device["residues"] == 2
+def test_exact_weights_survive_spills_and_prefixes(tctx, qp, oracle):
+    tctx.set_tuning(fold_weights=2)
+    # a budget that splits the live boundary to the host and back
+    assert tctx.contract_rows(14, device_budget_bytes=6 << 20).count == qp.known_count(14)
+    for prefix in ([5], [2, 9], [0, 7, 3]):
+        assert tctx.count(16, prefix) == oracle.contract(16, backend=oracle.PARALLEL_SORT_REDUCE, threads=8,
+                                                         symmetry=False, prefix=prefix)["count"]
+
+
+def test_fold_and_exact_weights_at_the_n20_bound(tctx, qp):
+    # Boards with up to 20 free rows use the one-plane accumulators: an N=20
+    # prefix slice, and an N=21 slice with one row placed (free rows 20).
+    got = []
+    for fold in (0, 1, 2):
+        tctx.set_tuning(fold_weights=fold)
+        got.append(tctx.count_with_stats(20, [3, 0, 7, 11]))
+    assert got[0][0] == got[1][0] == got[2][0]
+    got = []
+    for fold in (0, 2):
+        tctx.set_tuning(fold_weights=fold)
+        got.append(tctx.count_with_stats(21, [10, 3, 0, 8, 16]))
+    assert got[0][0] == got[1][0]
+    assert got[1][1].device["residues"] == 2
