@@ -289,7 +289,7 @@ struct Ctx {
     uint32_t fold_weights = 2;                  // 0 residues, 1 CRT fold, 2 exact 64-bit weights in the
                                                 // boundary (modes 1-2 only where exact: R = 2, N - k <= 20)
     double partition_fill = 0.83;               // starting value of Ctx::partition_fill
-    double slice_margin = 2.0;                  // predictive slicing: slice peak / mean slice peak
+    double slice_margin = 5.0;                  // predictive slicing: slice peak / mean slice peak
   } tune;
   DevBuf tail;                   // TailControl + overflow list
   uint64_t pool_gen = 0;         // bumped whenever a pool buffer is allocated or freed
