@@ -641,7 +641,8 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
           for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slots[l]], (unsigned long long)buf[l].res[r]);
         }
       }
-    __syncthreads();
+    // No barrier here: the list (and s_nused) is complete since the previous
+    // barrier, and the one below orders these additions before compaction.
     const u32 next = part + gridDim.x;
     if (next < parts) fetch(next);
     if (threadIdx.x == 0) {
