@@ -65,6 +65,28 @@ __device__ __forceinline__ void store_cand(Cand<R>* dst, const Cand<R>& c) {
   }
 }
 
+// L2 policy that keeps lines resident in preference to others: partition
+// tails are written 16 bytes at a time, and a line evicted before it is full
+// costs a DRAM read-fill and a second write-back.
+__device__ __forceinline__ u64 l2_keep_policy() {
+  u64 policy;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(policy));
+  return policy;
+}
+
+template <int R>
+__device__ __forceinline__ void store_cand_keep(Cand<R>* dst, const Cand<R>& c, u64 policy) {
+  u64 w01 = (u64)c.res[0] | (R > 1 ? (u64)c.res[R > 1 ? 1 : 0] << 32 : 0ull);
+  asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1, %2}, %3;" ::"l"(dst), "l"(c.key), "l"(w01), "l"(policy)
+               : "memory");
+  if constexpr (R > 2) {
+    u64 w23 = (u64)c.res[2] | (R > 3 ? (u64)c.res[R > 3 ? 3 : 2] << 32 : 0ull);
+    asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1, %2}, %3;" ::"l"(reinterpret_cast<char*>(dst) + 16),
+                 "l"(w23), "l"(0ull), "l"(policy)
+                 : "memory");
+  }
+}
+
 template <int R>
 __device__ __forceinline__ Cand<R> load_cand(const Cand<R>* src) {
   const ulonglong2* s = reinterpret_cast<const ulonglong2*>(src);
@@ -242,6 +264,7 @@ __global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_
   const u64 gwarp = (u64)blockIdx.x * WARPS + wid;
   const u64 stride = (u64)gridDim.x * WARPS * PW;
   bool overflow = false;
+  const u64 policy = l2_keep_policy();
 
   u64 nkey[kPPL], ckey[kPPL], fr[kPPL];
   u32 nw[kPPL][R], cw[kPPL][R];
@@ -251,9 +274,9 @@ __global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_
       const u64 i = base + q * 32 + lane;
       nkey[q] = kEmptyKey;
       if (i < n_in) {
-        nkey[q] = keys[i];
+        nkey[q] = __ldcs(keys + i);
 #pragma unroll
-        for (int r = 0; r < R; ++r) nw[q][r] = res[r * res_stride + i];
+        for (int r = 0; r < R; ++r) nw[q][r] = __ldcs(res + r * res_stride + i);
       }
     }
   };
@@ -312,7 +335,7 @@ __global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_
       for (int k = 0; k < kKB; ++k)
         if (part[k] != 0xffffffffu) {
           if (pos[k] < cap)
-            store_cand<R>(regions + (u64)part[k] * cap + pos[k], s_cand[wid][k * 32 + lane]);
+            store_cand_keep<R>(regions + (u64)part[k] * cap + pos[k], s_cand[wid][k * 32 + lane], policy);
           else
             overflow = true;
         }
