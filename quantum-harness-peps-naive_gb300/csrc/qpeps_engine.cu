@@ -408,6 +408,7 @@ struct Plan {
   int threads;
   unsigned tail_row;  // rows >= tail_row go to the slice-tail kernel (n = none)
   bool w64 = false;   // residue planes 0/1 hold the low/high words of exact weights (partitioned row merge)
+  int Rc = 0;         // residues of the CRT bookkeeping (= R except with w64, where R = 2 planes)
 };
 
 static size_t entry_bytes(const Plan& p) { return (size_t)(p.key_bits / 8) + 4u * p.R; }
@@ -440,6 +441,7 @@ static void sync_scalars(Ctx& ctx) {
 struct DevFrontier {
   u64 count = 0;
   u64 cap = 0;
+  u128 weight_bound = 0;  // upper bound of the live boundary's total weight (w64 certification)
 };
 
 // Boundary entries parked on the host (the seed, or a half split off under
@@ -449,12 +451,14 @@ struct HostChunk {
   bool row_counted = false;  // site grain: this row's metrics already include these entries
   bool no_tail = false;      // entries that overflowed the slice tail: contract every row here
   u64 count = 0;
+  u128 weight_bound = 0;      // upper bound of the chunk's total weight (w64 certification)
   std::vector<uint8_t> keys;
   std::vector<uint32_t> res;  // R planes of `count`
 };
 
 struct StepOut {
   u64 in = 0, terms = 0, out = 0;
+  u64 exact_sum = 0;  // w64: exact total weight of the output boundary
   u64 weight[kMaxResidues] = {0, 0, 0, 0};
   u64 final_sum[kMaxResidues] = {0, 0, 0, 0};
 };
@@ -642,7 +646,8 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     cudaEventElapsedTime(&ms_a, ctx.ev[0], ctx.ev[1]);
     cudaEventElapsedTime(&ms_b, ctx.ev[1], ctx.ev[2]);
     so.out = ctx.h_sc->out_count;
-    for (int r = 0; r < p.R; ++r) {
+    so.exact_sum = ctx.h_sc->weight_sum[0];
+    for (int r = 0; r < p.Rc; ++r) {
       // Exact weights: plane 0 carries the exact sums.
       so.weight[r] = ctx.h_sc->weight_sum[p.w64 ? 0 : r] % kPrimes[r];
       so.final_sum[r] = ctx.h_sc->final_sum[p.w64 ? 0 : r] % kPrimes[r];
@@ -693,6 +698,7 @@ static void split_to_host(Ctx& ctx, const Plan& p, DevFrontier& f, unsigned row,
   hc.row_counted = row_counted;
   hc.no_tail = no_tail;
   hc.count = moved;
+  hc.weight_bound = f.weight_bound;
   const size_t kb = key_bytes(p);
   hc.keys.resize(moved * kb);
   hc.res.resize((size_t)p.R * moved);
@@ -730,6 +736,7 @@ static void upload_chunk(Ctx& ctx, const Plan& p, const HostChunk& hc, DevFronti
   cuda_check(cudaStreamSynchronize(ctx.stream), "upload synchronize");
   ctx.h2d_bytes += hc.count * (kb + 4u * p.R);
   f.count = hc.count;
+  f.weight_bound = hc.weight_bound;
   if (ctx.rec) {
     GraphChunkRec c;
     c.count = hc.count;
@@ -743,6 +750,7 @@ static HostChunk chunk_from_items(const Plan& p, const std::vector<Item>& items,
   HostChunk hc;
   hc.row = row;
   hc.count = items.size();
+  for (const Item& it : items) hc.weight_bound += it.weight;
   const size_t kb = key_bytes(p);
   hc.keys.resize(hc.count * kb);
   hc.res.resize((size_t)p.R * hc.count);
@@ -884,22 +892,30 @@ static void run_chunks(Ctx& ctx, const Plan& p, std::vector<HostChunk> pending, 
           while (merge_step(ctx, p, f, true, site, fin, rs, row, &so) == StepStatus::NeedSplit)
             split_to_host(ctx, p, f, row, site, true, hc.no_tail, pending);
           if (fin)
-            for (int r = 0; r < p.R; ++r) rs.final_res[r] = (rs.final_res[r] + so.final_sum[r]) % kPrimes[r];
+            for (int r = 0; r < p.Rc; ++r) rs.final_res[r] = (rs.final_res[r] + so.final_sum[r]) % kPrimes[r];
         }
         site0 = 0;
         counted = false;
       } else {
+        if (p.w64) {
+          // Every entry has at most n - row successors, so the output's
+          // weights and per-key sums are at most (input total) * (n - row);
+          // the words hold them exactly while that stays below 2^63.
+          const u128 bound = f.weight_bound * (u128)(p.n - row);
+          if (bound >> 63) fail(QPEPS_ERR_OVERFLOW, row_msg("exact 64-bit weights are not certified at row", row + 1));
+        }
         while (merge_step(ctx, p, f, false, 0, last_row, rs, row, &so) == StepStatus::NeedSplit)
           split_to_host(ctx, p, f, row, 0, false, hc.no_tail, pending);
+        if (p.w64) f.weight_bound = so.exact_sum;
         acc.input_states += so.in;
         acc.candidates += (u128)so.in * p.n;
         acc.matched += so.terms;
         acc.completed += so.terms;
         if (last_row)
-          for (int r = 0; r < p.R; ++r) rs.final_res[r] = (rs.final_res[r] + so.final_sum[r]) % kPrimes[r];
+          for (int r = 0; r < p.Rc; ++r) rs.final_res[r] = (rs.final_res[r] + so.final_sum[r]) % kPrimes[r];
       }
       acc.output_states += last_row ? so.out : f.count;
-      for (int r = 0; r < p.R; ++r) acc.weight_res[r] = (acc.weight_res[r] + so.weight[r]) % kPrimes[r];
+      for (int r = 0; r < p.Rc; ++r) acc.weight_res[r] = (acc.weight_res[r] + so.weight[r]) % kPrimes[r];
       rs.peak_states = std::max<u64>(rs.peak_states, last_row ? so.out : f.count);
       acc.elapsed += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
@@ -996,10 +1012,17 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
     p.tail_row = n;  // auto: the merged row engine for every row (fastest measured through N=18)
   else
     p.tail_row = (tail_ok && o.tail_row < n) ? o.tail_row : n;
-  // Exact 64-bit weights: every weight and row sum is at most free_rows!
-  // (<= 20! < 2^63) and only the partitioned row merge reads the planes.
-  p.w64 = ctx.tune.fold_weights == 2 && ctx.tune.merge_kind == 1 && p.R == 2 && p.free_rows <= 20 &&
-          p.merge == QPEPS_MERGE_PARTITION && p.grain == QPEPS_GRAIN_ROW && p.key_bits == 64 && p.tail_row >= n;
+  // Exact 64-bit weights (only the partitioned row merge reads the planes):
+  // two u32 planes carry each weight's words and the host derives the Rc
+  // residues of the CRT bookkeeping from exact sums. Every row is certified
+  // before it runs from the exact total of its input (run_chunks); with at
+  // most 20 free rows that holds by 20! < 2^63, with 21 (Q(21)) it is checked.
+  p.Rc = p.R;
+  if (ctx.tune.fold_weights == 2 && ctx.tune.merge_kind == 1 && p.R >= 2 && p.free_rows <= 21 &&
+      p.merge == QPEPS_MERGE_PARTITION && p.grain == QPEPS_GRAIN_ROW && p.key_bits == 64 && p.tail_row >= n) {
+    p.w64 = true;
+    p.R = 2;
+  }
   return p;
 }
 
@@ -1012,7 +1035,7 @@ static void contract_items(Ctx& ctx, Contraction& out, const std::vector<Item>& 
     const u64 mask = (p.n >= 64) ? ~0ull : ((1ull << p.n) - 1);
     for (const Item& it : items)
       if (((u64)it.key & mask) == mask)
-        for (int r = 0; r < p.R; ++r)
+        for (int r = 0; r < p.Rc; ++r)
           out.rs.final_res[r] = (out.rs.final_res[r] + (u64)(it.weight % kPrimes[r])) % kPrimes[r];
     return;
   }
@@ -1126,6 +1149,7 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
   p.n = n;
   p.free_rows = n;
   p.R = crt_plan(n);
+  p.Rc = p.R;
   p.key_bits = 128;
   p.grain = QPEPS_GRAIN_SITE;
   p.merge = QPEPS_MERGE_HASH;
@@ -1597,8 +1621,8 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
   out.peak_states = std::max<u64>(out.peak_states, out.rs.peak_states);
   // Count: host-finished boards plus device final sums, then CRT.
   u64 res[kMaxResidues];
-  for (int r = 0; r < out.plan.R; ++r) res[r] = out.rs.final_res[r];
-  out.count = crt_reconstruct(res, out.plan.R);
+  for (int r = 0; r < out.plan.Rc; ++r) res[r] = out.rs.final_res[r];
+  out.count = crt_reconstruct(res, out.plan.Rc);
   if (out.count > factorial(out.plan.free_rows))
     fail(QPEPS_ERR_CRT_BOUND, "CRT reconstruction exceeds certified N! count bound");
   out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1607,8 +1631,8 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
 static u128 row_weight(const Contraction& c, const RowAcc& a) {
   if (!a.device_row) return a.weight_exact;
   u64 res[kMaxResidues];
-  for (int r = 0; r < c.plan.R; ++r) res[r] = a.weight_res[r];
-  return crt_reconstruct(res, c.plan.R);
+  for (int r = 0; r < c.plan.Rc; ++r) res[r] = a.weight_res[r];
+  return crt_reconstruct(res, c.plan.Rc);
 }
 
 static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_result* r, qpeps_layer* layers,
@@ -1648,7 +1672,7 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->row_operator_candidates = to_abi(cand);
   r->row_operator_matched = to_abi(matched);
   r->peak_rss_bytes = ctx.peak_pool_bytes;
-  r->residues = n ? (uint32_t)c.plan.R : 0;
+  r->residues = n ? (uint32_t)c.plan.Rc : 0;
   r->key_bits = n ? (uint32_t)c.plan.key_bits : 0;
   r->slice_depth = c.slice_depth;
   r->batches = c.rs.batches;
@@ -1670,8 +1694,8 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->h2d_bytes = c.h2d_bytes;
   r->d2h_bytes = c.d2h_bytes;
   for (int i = 0; i < kMaxResidues; ++i) {
-    r->residue_primes[i] = i < (n ? c.plan.R : 0) ? kPrimes[i] : 0;
-    r->count_residues[i] = i < (n ? c.plan.R : 0) ? (uint64_t)(c.count % kPrimes[i]) : 0;
+    r->residue_primes[i] = i < (n ? c.plan.Rc : 0) ? kPrimes[i] : 0;
+    r->count_residues[i] = i < (n ? c.plan.Rc : 0) ? (uint64_t)(c.count % kPrimes[i]) : 0;
   }
 }
 
@@ -1866,6 +1890,7 @@ static void serve_batch_loop(Server& sv) {
   p.n = 19;
   p.free_rows = 19;
   p.R = 2;
+  p.Rc = 2;
   p.key_bits = 64;
   p.grain = QPEPS_GRAIN_ROW;
   p.merge = QPEPS_MERGE_PARTITION;
