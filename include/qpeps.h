@@ -221,10 +221,12 @@ typedef struct qpeps_tuning {
   uint32_t wide_merge;           /* 0 never, 1 always, 2 auto: 8192-slot merge CTAs, 4096-candidate partitions */
   uint32_t wide_above_parts;     /* auto: 2048-candidate partition count above which merges go wide */
   uint32_t spread_cursors_below; /* partition counts up to which cursors get 32-byte spacing */
-  uint32_t fold_weights;         /* claim-list merge accumulator where weights fit (two residues,
-                                    N - k <= 20): 0 = two residue sums, 1 = one 64-bit CRT-folded
-                                    value per key, 2 = the boundary carries exact 64-bit weights
-                                    (default; the row merge only, else 1) */
+  uint32_t fold_weights;         /* 2 (default) = with the partitioned row merge and 13 <= N - k <= 21
+                                    the boundary carries exact 64-bit weights (each row certified
+                                    to stay below 2^63 before it runs, QPEPS_ERR_OVERFLOW
+                                    otherwise); 1 = residues, but with two residues (N - k <= 20)
+                                    the claim-list merge accumulates one CRT-folded 64-bit value
+                                    per key; 0 = residue sums throughout */
   double partition_fill;         /* mean candidates per partition / capacity, in [0.3, 0.95] */
   double slice_margin;           /* predictive slicing: assumed slice peak / mean slice peak, >= 1 */
 } qpeps_tuning;
