@@ -539,11 +539,14 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
 //      reduced back to residues on output;
 //   2: the two planes hold the low and high words of the exact weight, which
 //      is accumulated in a single 64-bit plane and written back as words.
-// Modes 1 and 2 are exact when every weight and every sum of weights stays
-// below p0 * p1 (about 4.6e18) and 2^63; the engine uses them for N <= 20. This is exact when every weight and every sum of
-// weights stays below p0 * p1 (about 4.6e18) and 2^64: a row's weights sum to
-// at most the number of partial placements, at most N! (20! = 2.4e18), so the
-// engine folds for N <= 20.
+// Mode 1 is exact while every weight and every per-key sum stays below
+// p0 * p1 (about 4.6e18): a row's weights sum to at most the number of
+// partial placements, at most (free rows)! (20! = 2.4e18), so the engine uses
+// it for boards with at most 20 free rows. Mode 2 is exact
+// while they stay below 2^63; the engine certifies that before every row from
+// the exact total of the row's input (at most that total times the free
+// columns), which holds for every board with at most 20 free rows and is
+// checked row by row at 21.
 // The one-plane accumulator value of a candidate's two u32 words.
 template <int kAcc>
 __device__ __forceinline__ u64 one_plane(u32 w0, u32 w1) {
