@@ -590,8 +590,10 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
 
   Cand<R> buf[LPT];
   u32 bcnt = 0;
-  auto fetch = [&](u32 part) {
-    bcnt = min(cursors[(u64)part * cstride], (u32)CAP);
+  // `cnt` is the partition's cursor, loaded one iteration ahead so that the
+  // candidate loads need not wait for it.
+  auto fetch = [&](u32 part, u32 cnt) {
+    bcnt = min(cnt, (u32)CAP);
     const Cand<R>* src = regions + (u64)part * CAP;
 #pragma unroll
     for (int l = 0; l < LPT; ++l) {
@@ -600,9 +602,11 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     }
   };
   u32 part = blockIdx.x;
-  if (part < parts) fetch(part);
+  if (part < parts) fetch(part, cursors[(u64)part * cstride]);
   __syncthreads();
   for (; part < parts; part += gridDim.x) {
+    const u32 next = part + gridDim.x;
+    const u32 next_cnt = next < parts ? cursors[(u64)next * cstride] : 0u;
     u32 slots[LPT];
     u32 fresh_bits = 0, dup_bits = 0;
 #pragma unroll
@@ -656,6 +660,15 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
         }
       }
     __syncthreads();
+    // The list (and s_nused) is complete since this barrier: reserve the
+    // partition's output range now, so the global atomic's round trip
+    // overlaps the repeated-key additions and the next partition's loads.
+    u32 n_unique = 0;
+    unsigned long long out_base = 0ull;
+    if (threadIdx.x == 0) {
+      n_unique = s_nused;
+      if (n_unique) out_base = atomicAdd(&sc->out_count, (unsigned long long)n_unique);
+    }
 #pragma unroll
     for (int l = 0; l < LPT; ++l)
       if ((dup_bits >> l) & 1u) {
@@ -667,14 +680,12 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
           for (int r = 0; r < R; ++r) atomicAdd(&s_acc[r * H + slots[l]], (unsigned long long)buf[l].res[r]);
         }
       }
-    // No barrier here: the list (and s_nused) is complete since the previous
-    // barrier, and the one below orders these additions before compaction.
-    const u32 next = part + gridDim.x;
-    if (next < parts) fetch(next);
+    // No barrier here: the barrier below orders these additions before
+    // compaction.
+    if (next < parts) fetch(next, next_cnt);
     if (threadIdx.x == 0) {
-      const u32 n = s_nused;
-      s_n = n;
-      s_base = n ? atomicAdd(&sc->out_count, (unsigned long long)n) : 0ull;
+      s_n = n_unique;
+      s_base = out_base;
       s_nused = 0;
     }
     __syncthreads();
