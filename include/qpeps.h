@@ -210,6 +210,10 @@ int qpeps_explicit_frontier(void* ctx, uint32_t n, uint32_t order, uint64_t supp
  * counts and metrics; only the speed changes. */
 #define QPEPS_SCATTER_SEARCH 0 /* shuffle search for each successor's parent */
 #define QPEPS_SCATTER_WINDOW 1 /* per-warp shared-memory candidate window (default) */
+#define QPEPS_SCATTER_TWO_LEVEL 2 /* coarse buckets, then partitions, each written as runs ordered in
+                                     shared memory (16-byte candidates, up to 2^20 partitions; the
+                                     window scatter elsewhere); needs about one more candidate array;
+                                     exact like the others, measured slower on GB300 */
 #define QPEPS_MERGEK_SCAN 0    /* ballot/scan compaction over the whole table */
 #define QPEPS_MERGEK_CLAIM 1   /* claim list + first-claimant stores (default) */
 

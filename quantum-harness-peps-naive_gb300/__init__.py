@@ -42,6 +42,7 @@ MERGE_HASH = 1
 MERGE_PARTITION = 2
 SCATTER_SEARCH = 0
 SCATTER_WINDOW = 1
+SCATTER_TWO_LEVEL = 2
 MERGEK_SCAN = 0
 MERGEK_CLAIM = 1
 

@@ -572,13 +572,19 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     u32 parts = 0, cstride = 1;
     u64 slots = 0;
     size_t table_bytes, region_bytes = 0;
+    PartitionCfg tl{};  // two-level scatter plan (tl.tl_nb = 0: one-level)
     if (partition) {
       const u64 parts64 = std::max<u64>(1, (u64)((double)so.terms / mean) + 1);
       if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
       parts = (u32)parts64;
+      if (ctx.tune.scatter_kind == 2 && two_level_plan(so.terms, parts, p.R, &tl)) parts = tl.parts;
       region_bytes = (size_t)parts * pcap * candidate_bytes(p.R);
       cstride = (parts <= ctx.tune.spread_cursors_below) ? 8u : 1u;
       table_bytes = region_bytes + ((size_t)parts * 4 * cstride + 255) / 256 * 256;
+      if (tl.tl_nb) {
+        tl.cursor_stride = cstride;
+        table_bytes += two_level_extra_bytes(tl);
+      }
     } else {
       slots = pow2_at_least(std::max<u64>(1024, so.terms * 2));
       table_bytes = slots * slot_bytes(p.key_bits, p.R);
@@ -606,6 +612,9 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane,
                     wide, ctx.tune.scatter_kind, ctx.tune.merge_kind,
                     p.w64 ? 2u : (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
+    pc.tl_nb = tl.tl_nb;
+    pc.tl_p2 = tl.tl_p2;
+    pc.tl_bcap = tl.tl_bcap;
     void* regions = ctx.table.ptr;
     uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
     if (partition)
@@ -2172,7 +2181,7 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
 
 static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.struct_size != sizeof(qpeps_tuning)) fail(QPEPS_ERR_INVALID, "qpeps_tuning.struct_size mismatch");
-  if (q.scatter_kind > 1) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0 or 1");
+  if (q.scatter_kind > 2) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0, 1 or 2");
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
@@ -2211,10 +2220,11 @@ static double autotune(Ctx& c, unsigned n, unsigned repeats, Ctx::Tune* best) {
   double best_ms = 1e300;
   Ctx::Tune best_t = saved;
   try {
-    for (uint32_t sk : {1u, 0u})
+    for (uint32_t sk : {1u, 0u, 2u})
       for (uint32_t ppl : {4u, 2u})
         for (uint32_t mk : {1u, 0u})
           for (double fill : {0.83, 0.9, 0.75}) {
+            if (sk == 2 && ppl != 4) continue;  // the two-level scatter has no parents-per-lane knob
             Ctx::Tune t = saved;
             t.scatter_kind = sk;
             t.parents_per_lane = ppl;

@@ -107,12 +107,17 @@ struct PartitionCfg {
                                   // two CTAs per SM; 1 = 1024 threads, 8192 slots, 4096 candidates,
                                   // one CTA per SM (R <= 2 only: the table is 8 KiB x (8 + 8R) bytes)
   uint32_t scatter_kind = 1;      // scatter: 0 = shuffle search for each successor's parent,
-                                  // 1 = per-warp shared-memory candidate window
+                                  // 1 = per-warp shared-memory candidate window,
+                                  // 2 = two-level (coarse buckets, then partitions; runs staged and
+                                  //     ordered in shared memory), where two_level_plan() accepts the step
   uint32_t merge_kind = 1;        // merge: 0 = ballot/scan compaction over the whole table,
                                   // 1 = claim list + first-claimant stores (three phases)
   uint32_t fold = 0;              // merge_kind 1, R = 2, one 64-bit accumulator plane:
                                   // 1 = CRT-folded residues, 2 = the planes hold an exact weight's
                                   // low and high words (both exact only when N! < p0 * p1, N <= 20)
+  uint32_t tl_nb = 0;             // two-level scatter: coarse buckets (0 = one-level scatter)
+  uint32_t tl_p2 = 0;             // two-level scatter: partitions per bucket (parts = tl_nb * tl_p2)
+  uint64_t tl_bcap = 0;           // two-level scatter: candidate slots per bucket
 };
 
 size_t candidate_bytes(int residues);
@@ -120,6 +125,16 @@ size_t candidate_bytes(int residues);
 uint32_t partition_capacity(uint32_t wide = 0);
 // Whether the wide merge shape is available for a residue count.
 bool wide_merge_supported(int residues);
+
+// Two-level scatter plan for a step of `terms` successors and at least
+// `parts` partitions: sets tl_nb, tl_p2, tl_bcap and parts (= tl_nb * tl_p2,
+// rounded up from `parts`). False where it does not apply (more than 16-byte
+// candidates, or more partitions than its bins address).
+bool two_level_plan(uint64_t terms, uint32_t parts, int residues, PartitionCfg* pc);
+// Its scratch follows the partition cursors (parts x 4 x cursor_stride bytes,
+// rounded up to 256) in the same allocation: bucket cursors, then bucket slots.
+size_t two_level_cursor_bytes(const PartitionCfg& pc);
+size_t two_level_extra_bytes(const PartitionCfg& pc);
 
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* scalars, cudaStream_t stream);

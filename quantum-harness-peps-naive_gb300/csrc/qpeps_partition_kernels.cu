@@ -15,6 +15,9 @@
 // the order of the output boundary is not observable by any metric.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+
 #include "qpeps_device.cuh"
 #include "qpeps_internal.h"
 
@@ -749,6 +752,356 @@ __global__ void __launch_bounds__(BLOCK) slot_count_kernel(const u64* __restrict
   if (threadIdx.x == 0 && t) atomicAdd(&sc->terms, t);
 }
 
+// ---------------------------------------------------------------------------
+// Two-level scatter (scatter_kind 2, 16-byte candidates). The one-level
+// scatters store every candidate on its own to a random partition tail (one
+// cursor atomic and one scattered 16-byte store each). Here a CTA stages a
+// round of up to kTlNC candidates in shared memory, orders them by
+// destination, reserves one range per destination with one global atomic and
+// writes each destination's candidates as one contiguous run:
+//   level 1 (bucket_scatter_kernel): parents -> nb coarse buckets,
+//            bucket = partition / p2;
+//   level 2 (bucket_split_kernel): each bucket's candidates -> its p2
+//            partitions, partition = bucket * p2 + sub-bucket.
+// Every candidate ends in partition_of(fib_hash_a(key), parts), the partition
+// the one-level scatters give it, so the merge is unchanged. Capacity rules
+// are the same: a bucket or partition never receives more than it holds, and
+// the error word is set instead.
+// Measured on GB300, exact Q(18) with the default tuning otherwise: level 1 +
+// level 2 take 661 ms against the window scatter's 605 ms (Q(17): 54 + 35 ms
+// against 80 ms). The two staging passes move every candidate twice at about
+// 2.8 TB/s, which costs more than the scattered stores they replace; the
+// window scatter stays the default and this one is a tuning choice.
+
+constexpr int kTlMaxBins = 1024;  // nb and p2 limit
+constexpr int kTlPPT = 2;         // level 1: parents per thread per chunk
+
+// CTA shape: BLOCK threads stage kNC candidates a round, kMinBlocks CTAs
+// per SM. (One 1024-thread CTA per SM staging 6144 candidates measured
+// slower: its phases cannot overlap.)
+template <int BLOCK>
+struct TlShape;
+template <>
+struct TlShape<512> {
+  static constexpr int kNC = 2560, kMinBlocks = 2;
+};
+constexpr int kTlBlock = 512;
+
+template <int R, int BLOCK>
+constexpr size_t tl_smem() {
+  // staged (generation order) + staged (destination order) + destination of
+  // each ordered slot + per-bin count, offset and reserved base
+  return (size_t)TlShape<BLOCK>::kNC * (sizeof(Cand<R>) * 2 + 2) + (size_t)kTlMaxBins * 4 * 3;
+}
+
+// Exclusive scan of one u32 per thread over a BLOCK-thread CTA; *total
+// receives the sum. Contains two barriers.
+template <int BLOCK>
+__device__ __forceinline__ u32 tl_block_scan(u32 v, u32* s_warp, u32* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  u32 incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const u32 t = __shfl_up_sync(kFullMask, incl, d);
+    if (lane >= d) incl += t;
+  }
+  if (lane == 31) s_warp[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const u32 w = lane < BLOCK / 32 ? s_warp[lane] : 0u;
+    u32 wi = w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const u32 t = __shfl_up_sync(kFullMask, wi, d);
+      if (lane >= d) wi += t;
+    }
+    s_warp[lane] = wi - w;
+    if (lane == 31) *total = wi;
+  }
+  __syncthreads();
+  return s_warp[wid] + incl - v;
+}
+
+// Order the m staged candidates by bin (fetch_of(k, i) is candidate
+// i = k * BLOCK + tid, with bin[k] and rank[k]), reserve each bin's range with one atomic on
+// cursors[bin_cursor(bin)], and write the runs to dst(bin) + base + rank.
+// Shared by both levels; ends with a barrier, after which s_a, s_b and the
+// bin arrays may be reused.
+template <int R, int BLOCK, int PER, typename FetchOf, typename CursorOf, typename DestOf>
+__device__ __forceinline__ void tl_order_and_write(FetchOf fetch_of, Cand<R>* s_b, unsigned short* s_bin, u32* s_cnt,
+                                                   u32* s_off, u32* s_base, u32* s_warp, u32* s_total, u32 m,
+                                                   u32 nbins, const u32 (&bin)[PER], const u32 (&rank)[PER],
+                                                   CursorOf cursor_of, DestOf dest_of, u64 cap, u64 policy,
+                                                   bool& overflow) {
+  const int tid = threadIdx.x;
+  __syncthreads();  // every rank is taken
+  // Bins are dealt to threads in blocks of kTlMaxBins / BLOCK consecutive
+  // bins, so the scan order is the bin order.
+  constexpr int BPT = kTlMaxBins / BLOCK;
+  static_assert(kTlMaxBins % BLOCK == 0, "bins per thread");
+  u32 c[BPT];
+  u32 mine = 0;
+#pragma unroll
+  for (int q = 0; q < BPT; ++q) {
+    const u32 bn = (u32)tid * BPT + q;
+    c[q] = bn < nbins ? s_cnt[bn] : 0u;
+    mine += c[q];
+  }
+  u32 off = tl_block_scan<BLOCK>(mine, s_warp, s_total);
+#pragma unroll
+  for (int q = 0; q < BPT; ++q) {
+    const u32 bn = (u32)tid * BPT + q;
+    if (bn < nbins) {
+      s_off[bn] = off;
+      if (c[q]) s_base[bn] = atomicAdd(cursor_of(bn), c[q]);
+      off += c[q];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const u32 i = (u32)k * BLOCK + tid;
+    if (i < m) {
+      const u32 j = s_off[bin[k]] + rank[k];
+      s_b[j] = fetch_of(k, i);
+      s_bin[j] = (unsigned short)bin[k];
+    }
+  }
+  __syncthreads();
+  for (u32 j = tid; j < m; j += BLOCK) {
+    const u32 b = s_bin[j];
+    const u64 pos = (u64)s_base[b] + (j - s_off[b]);
+    if (pos < cap)
+      store_cand_keep<R>(dest_of(b) + pos, s_b[j], policy);
+    else
+      overflow = true;
+  }
+  __syncthreads();
+}
+
+// Level 1. Parents stream through each CTA in chunks of kTlPPT * BLOCK (the
+// next chunk is loaded into registers while the current one is staged); a
+// chunk's successors, flattened in parent order and lowest free column first,
+// fill rounds of exactly kNC staged candidates across chunk boundaries (only
+// the CTA's last round is partial).
+template <int R, int BLOCK, typename Layout>
+__global__ void __launch_bounds__(BLOCK, TlShape<BLOCK>::kMinBlocks) bucket_scatter_kernel(
+    const u64* __restrict__ keys, const u32* __restrict__ res, u64 res_stride, u64 n_in, Layout L,
+    Cand<R>* __restrict__ buckets, u64 bcap, u32* __restrict__ bcur, u32 nb, u32 parts, u32 p2,
+    StepScalars* __restrict__ sc) {
+  constexpr int kTlNC = TlShape<BLOCK>::kNC, kTlPer = kTlNC / BLOCK;
+  static_assert(kTlNC % BLOCK == 0, "two-level shape");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cand<R>* s_a = reinterpret_cast<Cand<R>*>(smem_raw);
+  Cand<R>* s_b = s_a + kTlNC;
+  unsigned short* s_bin = reinterpret_cast<unsigned short*>(s_b + kTlNC);
+  u32* s_cnt = reinterpret_cast<u32*>(s_bin + kTlNC);
+  u32* s_off = s_cnt + kTlMaxBins;
+  u32* s_base = s_off + kTlMaxBins;
+  __shared__ u32 s_warp[32];
+  __shared__ u32 s_total;
+  const int tid = threadIdx.x;
+  constexpr u64 CP = (u64)kTlPPT * BLOCK;
+  const u64 stride = (u64)gridDim.x * CP;
+  const u64 policy = l2_keep_policy();
+  bool overflow = false;
+
+  // Current chunk (free masks computed) and the next one (raw, in flight).
+  u64 ck[kTlPPT], cf[kTlPPT], nk[kTlPPT];
+  u32 cw[kTlPPT][R], nw[kTlPPT][R];
+  auto prefetch = [&](u64 base) {
+#pragma unroll
+    for (int q = 0; q < kTlPPT; ++q) {
+      const u64 i = base + (u64)q * BLOCK + tid;
+      nk[q] = kEmptyKey;
+      if (i < n_in) {
+        nk[q] = __ldcs(keys + i);
+#pragma unroll
+        for (int r = 0; r < R; ++r) nw[q][r] = __ldcs(res + r * res_stride + i);
+      }
+    }
+  };
+  u64 next_base = (u64)blockIdx.x * CP;
+  bool more = next_base < n_in;  // a loaded chunk is waiting (uniform over the CTA)
+  if (more) prefetch(next_base);
+  u32 first = 0, total = 0, r0 = 0;  // this thread's first successor index; chunk total; consumed
+  // Make the waiting chunk current and start loading the one after it.
+  // Uniform; two barriers (the scan).
+  auto advance = [&]() {
+    u32 cnt = 0;
+#pragma unroll
+    for (int q = 0; q < kTlPPT; ++q) {
+      ck[q] = nk[q];
+#pragma unroll
+      for (int r = 0; r < R; ++r) cw[q][r] = nw[q][r];
+      cf[q] = 0;
+      if (ck[q] != kEmptyKey) {
+        const State s = L.unpack(ck[q]);
+        cf[q] = ~(s.cols | s.dr | s.dl) & L.mask_of(ck[q]);
+      }
+      cnt += (u32)__popcll(cf[q]);
+    }
+    next_base += stride;
+    more = next_base < n_in;
+    if (more) prefetch(next_base);
+    first = tl_block_scan<BLOCK>(cnt, s_warp, &s_total);
+    total = s_total;
+    r0 = 0;
+  };
+  // Stage successors [lo, lo + take) of the current chunk at s_a[at, at + take).
+  auto stage = [&](u32 lo, u32 take, u32 at) {
+    u32 g = first;
+#pragma unroll
+    for (int q = 0; q < kTlPPT; ++q) {
+      const u32 c = (u32)__popcll(cf[q]);
+      if (c && g + c > lo && g < lo + take) {
+        const State s = L.unpack(ck[q]);
+        u64 f = cf[q];
+        u32 j = g;
+        while (f) {
+          const u64 b = f & (0ull - f);
+          f ^= b;
+          if (j >= lo && j < lo + take) {
+            Cand<R> cd;
+            cd.key = L.successor(ck[q], s, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) cd.res[r] = cw[q][r];
+            s_a[at + (j - lo)] = cd;
+          }
+          ++j;
+        }
+      }
+      g += c;
+    }
+  };
+  for (;;) {
+    u32 m = 0;  // staged this round (uniform)
+    for (;;) {
+      if (r0 == total) {
+        if (!more) break;
+        advance();
+        continue;
+      }
+      const u32 take = min(total - r0, (u32)kTlNC - m);
+      stage(r0, take, m);
+      m += take;
+      r0 += take;
+      if (m == (u32)kTlNC) break;
+    }
+    if (m == 0) break;
+    for (u32 i = tid; i < nb; i += BLOCK) s_cnt[i] = 0u;
+    __syncthreads();  // staged candidates and cleared counts
+    u32 bin[kTlPer], rank[kTlPer];
+#pragma unroll
+    for (int k = 0; k < kTlPer; ++k) {
+      const u32 i = (u32)k * BLOCK + tid;
+      bin[k] = 0;
+      rank[k] = 0;
+      if (i < m) {
+        bin[k] = partition_of(fib_hash_a(s_a[i].key), parts) / p2;
+        if (bin[k] >= nb) {  // cannot happen (parts = nb * p2); kept off shared memory all the same
+          bin[k] = 0;
+          overflow = true;
+        }
+        rank[k] = atomicAdd(&s_cnt[bin[k]], 1u);
+      }
+    }
+    tl_order_and_write<R, BLOCK, kTlPer>(
+        [&](int, u32 i) { return s_a[i]; }, s_b, s_bin, s_cnt, s_off, s_base, s_warp, &s_total, m, nb, bin, rank,
+        [&](u32 b) { return bcur + b; }, [&](u32 b) { return buckets + (u64)b * bcap; }, bcap, policy, overflow);
+  }
+  if (overflow) atomicOr(&sc->error, kErrOverflow);
+}
+
+// Level 2. Work item = (bucket, chunk of kNC candidates); the candidates
+// stay in registers until they are ordered.
+template <int R, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, TlShape<BLOCK>::kMinBlocks) bucket_split_kernel(const Cand<R>* __restrict__ buckets, u64 bcap,
+                                                                   const u32* __restrict__ bcur, u32 nb,
+                                                                   u32 chunks_per_bucket, u32 parts, u32 p2,
+                                                                   Cand<R>* __restrict__ regions, u32 cap,
+                                                                   u32* __restrict__ cursors, u32 cstride,
+                                                                   StepScalars* __restrict__ sc) {
+  constexpr int kTlNC = TlShape<BLOCK>::kNC, kTlPer = kTlNC / BLOCK;
+  static_assert(kTlNC % BLOCK == 0, "two-level shape");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cand<R>* s_b = reinterpret_cast<Cand<R>*>(smem_raw) + kTlNC;  // same layout as level 1
+  unsigned short* s_bin = reinterpret_cast<unsigned short*>(s_b + kTlNC);
+  u32* s_cnt = reinterpret_cast<u32*>(s_bin + kTlNC);
+  u32* s_off = s_cnt + kTlMaxBins;
+  u32* s_base = s_off + kTlMaxBins;
+  __shared__ u32 s_warp[32];
+  __shared__ u32 s_total;
+  const int tid = threadIdx.x;
+  const u64 policy = l2_keep_policy();
+  bool overflow = false;
+  const u64 items = (u64)nb * chunks_per_bucket;
+  for (u64 it = blockIdx.x; it < items; it += gridDim.x) {
+    const u32 b = (u32)(it / chunks_per_bucket);
+    const u64 lo = (it % chunks_per_bucket) * (u64)kTlNC;
+    const u64 nbk = min((u64)bcur[b], bcap);
+    if (lo >= nbk) continue;  // uniform over the CTA
+    const u32 m = (u32)min(nbk - lo, (u64)kTlNC);
+    for (u32 i = tid; i < p2; i += BLOCK) s_cnt[i] = 0u;
+    const Cand<R>* src = buckets + (u64)b * bcap + lo;
+    Cand<R> c[kTlPer];
+#pragma unroll
+    for (int k = 0; k < kTlPer; ++k) {
+      const u32 i = (u32)k * BLOCK + tid;
+      if (i < m) c[k] = load_cand<R>(src + i);
+    }
+    __syncthreads();  // cleared counts
+    u32 bin[kTlPer], rank[kTlPer];
+#pragma unroll
+    for (int k = 0; k < kTlPer; ++k) {
+      const u32 i = (u32)k * BLOCK + tid;
+      bin[k] = 0;
+      rank[k] = 0;
+      if (i < m) {
+        bin[k] = partition_of(fib_hash_a(c[k].key), parts) - b * p2;
+        if (bin[k] >= p2) {  // not this bucket's: cannot happen; flag it rather than index past the bins
+          bin[k] = 0;
+          overflow = true;
+        }
+        rank[k] = atomicAdd(&s_cnt[bin[k]], 1u);
+      }
+    }
+    tl_order_and_write<R, BLOCK, kTlPer>(
+        [&](int k, u32) { return c[k]; }, s_b, s_bin, s_cnt, s_off, s_base, s_warp, &s_total, m, p2, bin, rank,
+        [&](u32 s) { return cursors + (u64)(b * p2 + s) * cstride; },
+        [&](u32 s) { return regions + (u64)(b * p2 + s) * cap; }, (u64)cap, policy, overflow);
+  }
+  if (overflow) atomicOr(&sc->error, kErrOverflow);
+}
+
+template <int R, int BLOCK, typename Layout>
+cudaError_t two_level_scatter(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
+                              u32* cursors, StepScalars* sc, cudaStream_t stream) {
+  char* area = reinterpret_cast<char*>(cursors) + two_level_cursor_bytes(pc);
+  u32* bcur = reinterpret_cast<u32*>(area);
+  Cand<R>* buckets = reinterpret_cast<Cand<R>*>(area + (((size_t)pc.tl_nb * 4 + 255) / 256) * 256);
+  cudaError_t e = cudaMemsetAsync(bcur, 0, (size_t)pc.tl_nb * 4, stream);
+  if (e != cudaSuccess) return e;
+  constexpr int kTlNC = TlShape<BLOCK>::kNC, kMinBlocks = TlShape<BLOCK>::kMinBlocks;
+  constexpr size_t smem = tl_smem<R, BLOCK>();
+  auto k1 = bucket_scatter_kernel<R, BLOCK, Layout>;
+  auto k2 = bucket_split_kernel<R, BLOCK>;
+  if ((e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) return e;
+  const u64 chunks1 = (n_in + (u64)kTlPPT * BLOCK - 1) / ((u64)kTlPPT * BLOCK);
+  const unsigned g1 = (unsigned)std::max<u64>(1, std::min<u64>(chunks1, (u64)pc.sms * kMinBlocks));
+  k1<<<g1, BLOCK, smem, stream>>>(reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, buckets,
+                                     pc.tl_bcap, bcur, pc.tl_nb, pc.parts, pc.tl_p2, sc);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const u32 cpb = (u32)((pc.tl_bcap + kTlNC - 1) / kTlNC);
+  const u64 items = (u64)pc.tl_nb * cpb;
+  const unsigned g2 = (unsigned)std::max<u64>(1, std::min<u64>(items, (u64)pc.sms * kMinBlocks));
+  k2<<<g2, BLOCK, smem, stream>>>(buckets, pc.tl_bcap, bcur, pc.tl_nb, cpb, pc.parts, pc.tl_p2,
+                                     reinterpret_cast<Cand<R>*>(regions), pc.cap, cursors,
+                                     pc.cursor_stride ? pc.cursor_stride : 1, sc);
+  return cudaGetLastError();
+}
+
 constexpr int kScatterBlock = 256;
 // Merge CTA shapes: table slots H, candidate capacity H / 2.
 constexpr int kMergeBlock = 512, kMergeH = 4096;
@@ -765,7 +1118,7 @@ cudaError_t scatter_ppl(const PartitionCfg& pc, const FrontierView& in, u64 n_in
   u64 want = (n_in + kScatterBlock * PPL - 1) / (kScatterBlock * PPL);
   const u64 capb = (u64)pc.sms * 8;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
-  if (pc.scatter_kind == 1) {
+  if (pc.scatter_kind != 0) {  // 2 without a two-level plan: the window scatter
     partition_scatter_list_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
         reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
         pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
@@ -853,9 +1206,46 @@ cudaError_t launch_serve_merge(const PartitionCfg& pc, const void* regions, cons
 uint32_t partition_capacity(uint32_t wide) { return wide ? kWideH / 2 : kMergeH / 2; }
 bool wide_merge_supported(int residues) { return residues >= 1 && residues <= 2; }
 
+size_t two_level_cursor_bytes(const PartitionCfg& pc) {
+  return ((size_t)pc.parts * 4 * (pc.cursor_stride ? pc.cursor_stride : 1) + 255) / 256 * 256;
+}
+
+size_t two_level_extra_bytes(const PartitionCfg& pc) {
+  return ((size_t)pc.tl_nb * 4 + 255) / 256 * 256 + (size_t)pc.tl_nb * pc.tl_bcap * 16;
+}
+
+bool two_level_plan(uint64_t terms, uint32_t parts, int residues, PartitionCfg* pc) {
+  if (residues > 2 || terms == 0 || parts == 0 || (u64)parts > (u64)kTlMaxBins * kTlMaxBins) return false;
+  u64 nb = (u64)std::llround(std::sqrt((double)parts));
+  nb = std::min<u64>(std::max<u64>(nb, 1), kTlMaxBins);
+  u64 p2 = (parts + nb - 1) / nb;
+  if (p2 > (u64)kTlMaxBins) {
+    nb = (parts + kTlMaxBins - 1) / kTlMaxBins;
+    p2 = (parts + nb - 1) / nb;
+  }
+  if (nb > (u64)kTlMaxBins || p2 > (u64)kTlMaxBins) return false;
+  // Hash buckets: mean terms / nb, standard deviation about its square root.
+  const double mean = (double)terms / (double)nb;
+  const u64 bcap = (u64)(mean * 1.01 + 8.0 * std::sqrt(mean)) + 1024;
+  if (bcap >= 0xffffffffull) return false;  // bucket cursors are u32
+  pc->tl_nb = (u32)nb;
+  pc->tl_p2 = (u32)p2;
+  pc->tl_bcap = bcap;
+  pc->parts = (u32)(nb * p2);
+  return true;
+}
+
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
+  if (pc.tl_nb) {
+    if (pc.tl_nb > (u32)kTlMaxBins || pc.tl_p2 > (u32)kTlMaxBins || pc.parts != pc.tl_nb * pc.tl_p2)
+      return cudaErrorInvalidValue;
+    const FixedLayout L{n, pboard_mask_host(n)};
+    if (pc.residues == 1) return two_level_scatter<1, kTlBlock>(pc, in, n_in, L, regions, cursors, sc, stream);
+    if (pc.residues == 2) return two_level_scatter<2, kTlBlock>(pc, in, n_in, L, regions, cursors, sc, stream);
+    return cudaErrorInvalidValue;
+  }
   switch (pc.residues) {
     case 1: return scatter_impl<1>(pc, in, n_in, FixedLayout{n, pboard_mask_host(n)}, regions, cursors, sc, stream);
     case 2: return scatter_impl<2>(pc, in, n_in, FixedLayout{n, pboard_mask_host(n)}, regions, cursors, sc, stream);

@@ -34,7 +34,7 @@ def tctx(qp):
 
 
 @pytest.mark.parametrize("scatter,ppl,merge,wide,fold", [
-    combo for combo in itertools.product((0, 1), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
+    combo for combo in itertools.product((0, 1, 2), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
 ])
 def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold):
     tctx.set_tuning(scatter_kind=scatter, parents_per_lane=ppl, merge_kind=merge, wide_merge=wide,
@@ -45,6 +45,38 @@ def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wi
         assert got.count == want["count"]
         assert got.peak_states == want["peak_states"]
         assert [l.output_states for l in got.layers] == [l["output_states"] for l in want["layers"]]
+
+
+@pytest.mark.parametrize("n", [15, 16, 17])
+def test_two_level_scatter_equals_the_window_scatter(tctx, qp, n):
+    # Coarse buckets then partitions, each written as ordered runs: the same
+    # partitions, so the same boundary, counts and per-row metrics.
+    ref = tctx.contract_rows(n)
+    tctx.set_tuning(scatter_kind=qp.SCATTER_TWO_LEVEL)
+    got = tctx.contract_rows(n)
+    assert got.count == ref.count == qp.known_count(n)
+    assert _layers(got) == _layers(ref)
+    assert got.peak_states == ref.peak_states
+    first = tctx.contract_rows(n, use_graph=1)
+    replay = tctx.contract_rows(n, use_graph=1)
+    assert first.count == replay.count == qp.known_count(n)
+    assert _layers(replay) == _layers(ref)
+
+
+def test_two_level_scatter_residues_budgets_and_prefixes(tctx, qp, oracle):
+    tctx.set_tuning(scatter_kind=qp.SCATTER_TWO_LEVEL)
+    # One residue plane (N <= 12) and exact weights use 16-byte candidates;
+    # three or four planes (32-byte candidates) keep the window scatter.
+    for residues in (1, 2):
+        assert tctx.contract_rows(12, residues=residues).count == qp.known_count(12)
+    tctx.set_tuning(fold_weights=0)
+    for residues in (2, 3, 4):
+        assert tctx.contract_rows(12, residues=residues).count == qp.known_count(12)
+    tctx.set_tuning(fold_weights=2, partition_fill=0.3, spread_cursors_below=0)
+    assert tctx.contract_rows(14, device_budget_bytes=8 << 20).count == qp.known_count(14)
+    for n, prefix in [(14, [3, 0]), (15, [7, 2, 4])]:
+        want = oracle.contract(n, symmetry=False, prefix=prefix)["count"]
+        assert tctx.count(n, prefix) == want
 
 
 def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
@@ -58,7 +90,7 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 
 @pytest.mark.parametrize("field,value", [
-    ("scatter_kind", 2), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
+    ("scatter_kind", 3), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
     ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 3),
 ])
 def test_out_of_range_tuning_is_rejected_and_kept(tctx, qp, field, value):
