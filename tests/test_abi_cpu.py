@@ -74,3 +74,17 @@ def test_tuning_default_is_the_library_default(qp):
     assert t["wide_merge"] == 2
     assert 0.3 <= t["partition_fill"] <= 0.95
     assert t["slice_margin"] >= 1.0
+
+
+def test_no_host_fallback_without_a_device(qp):
+    # The library computes only on the GPU: without a CUDA device, creating a
+    # context (and so any contraction) fails with QPEPS_ERR_CUDA instead of
+    # running on the host.
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(qp.ContractionError) as e:
+        qp.Context(0)
+    assert e.value.code == qp.QPEPS_ERR_CUDA
+    with pytest.raises(qp.ContractionError):
+        qp.contract_rows(8)
