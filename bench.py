@@ -10,25 +10,34 @@ whole contraction on the device from its seeds (checked row by row against the
 recorded run); --no-graph contracts eagerly every step.
 
 value  : boundary entries per second = (boundary entries of the merged
-         contraction: the sum over rows of the merged frontier's input states)
-         / (device time of the whole contraction, CUDA events on the
-         library's stream). When the library slices the frontier into device
-         batches it processes more entries than that (lost merges); those
-         are reported as boundary_entries_processed_per_step and do not
-         inflate `value`.
+         contraction: the sum over device rows of the merged frontier's input
+         states, the reference's LayerMetric.input_states) / (device time of
+         the whole contraction, CUDA events on the library's stream). The
+         merged figure is measured in the same run: one untimed contraction
+         on a separate context with the whole frontier in one device batch.
+         When the timed steps slice the frontier into several device batches
+         they process more entries (lost merges); those are reported as
+         boundary_entries_processed_per_step and do not inflate `value`.
 e2e    : the same entries / wall time of the C-ABI call (host seeding,
          host->device upload of the seed boundary, all row steps, device->host
          read-back of every row's metrics and of the count residues).
-roofline: the merge step (scatter + merge kernels, plus the row count),
-         algorithmic bytes E*(S_in+S_out) summed over the row steps of one
-         contraction over those kernels' CUDA-event time; `traffic` is the DRAM
-         bytes ncu measured over all scatter and merge launches of one Q(18)
-         contraction with the default tuning.
+roofline: the merge step (scatter + merge kernels), algorithmic bytes
+         E*(S_in+S_out) summed over the row steps of one contraction over
+         those kernels' CUDA-event time. `traffic` is DRAM bytes per step
+         scaled from a small ncu capture of peak-row launches (see
+         TRAFFIC_PER_ALGORITHMIC_BYTE); null where none applies.
 cpu_baseline: the CPU oracle (threaded restatement of the reference's
-         sort-reduce driver) on the first rows of the same workload.
+         sort-reduce driver) on the first rows of the same workload, median of
+         three samples.
+same_workload: the full Q(16) contraction on both the GPU (this library) and
+         the CPU oracle (all host threads, median of three), so that the two
+         rates compare identical work.
+serve  : a short seeded Poisson stream through the continuous-batching server
+         (--serve runs the full 10,000-request stream on its own).
 
 --impl reference times only that CPU restatement (there is no runnable
-reference binary: the reference is Rust and no Rust toolchain exists here).
+reference binary: the reference is Rust and no Rust toolchain exists here),
+with the same `config` as this arm and each step a bounded sample of it.
 Inputs are synthetic by construction: the workload is the empty N x N board.
 """
 from __future__ import annotations
@@ -50,15 +59,11 @@ sys.path.insert(0, str(ROOT / "oracle"))
 
 PACKAGE = "quantum-harness-peps-naive_gb300"
 
-# Boundary entries of the merged contraction of Q(N): the sum over rows of the
-# merged frontier's input states (the reference's LayerMetric.input_states),
-# i.e. the work unit of "boundary entries/s", independent of how a run slices
-# the frontier. N <= 16 match the CPU oracle; 17 and 18 were measured by this
-# library in single-batch merged runs (tail_row off, one device batch).
-MERGED_ENTRIES = {16: 397600651, 17: 2684482260, 18: 16682949222}
-# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) over every
-# partition scatter and merge launch of one contraction, default tuning.
-DRAM_TRAFFIC_PER_STEP = {18: 1873.1e9}
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
+# byte of the merge step, from a capture of a few peak-row scatter and merge
+# launches (profiles/); the bench scales the contraction's algorithmic bytes
+# by it. Keyed by the scatter kind the figure was captured with.
+TRAFFIC_PER_ALGORITHMIC_BYTE: dict = {}
 METRIC = "Q(N) wall time & boundary entries/s at N=18 (bit-exact)"
 UNIT = "boundary entries/s"
 
@@ -161,6 +166,18 @@ def max_over_ranks(values, device="cpu"):
     return [float(x) for x in t.tolist()]
 
 
+def workload_config(args) -> dict:
+    """The workload both arms report: what is computed, not how this run did it."""
+    world, _, _ = dist_env()
+    return {
+        "workload": f"Q({args.n}) exact, all first-row orbit slices",
+        "n": args.n,
+        "grain": args.grain,
+        "l2": "inputs larger than L2 (boundary buffers of GBs per row)",
+        "parallelism": "replicas" if world > 1 else "single",
+    }
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -188,15 +205,73 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "u64 keys + u128 checked coefficients",
-        "data": "synthetic (empty N x N board)",
-        "config": {"workload": f"Q({args.n}) orbit-sliced row contraction, first {args.cpu_rows} rows",
-                   "n": args.n, "rows": args.cpu_rows},
+        "data": "synthetic (empty N x N board; the workload has no external input)",
+        "config": workload_config(args),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"first {args.cpu_rows} rows of Q({args.n}) ({entries} boundary entries), "
-                                   f"threaded C++ restatement of contract_rows_d4_orbit_parallel_sort_reduce"},
+                         "sample": f"first {args.cpu_rows} rows of Q({args.n}) ({entries} boundary entries) per step, "
+                                   f"threaded C++ restatement of contract_rows_d4_orbit_parallel_sort_reduce "
+                                   f"(src/lib.rs:5469-5626); median of {args.steps} steps"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def merged_entries(pkg, n: int, device: int, opts: dict):
+    """Boundary entries of the merged contraction of Q(n): one untimed
+    contraction with the whole frontier in one device batch (slice_depth 1:
+    only the first row on the host) on a context of its own, closed
+    afterwards. None when that batch does not fit the device."""
+    c = pkg.Context(device)
+    try:
+        r = c.contract_rows(n, slice_depth=1, use_graph=0,
+                            **{k: v for k, v in opts.items() if k not in ("use_graph", "slice_depth")})
+        if r.count != pkg.known_count(n) or r.device["batches"] != 1:
+            return None
+        return r.device["entries_in"]
+    except pkg.ContractionError:
+        return None
+    finally:
+        c.close()
+
+
+def same_workload_pair(pkg, ctx, n: int, threads: int, steps: int = 5, cpu_repeats: int = 3) -> dict:
+    """Full Q(n) on the GPU (CUDA-graph replay, median wall of `steps`) and on
+    the CPU oracle (all host threads, median of `cpu_repeats`)."""
+    import oracle_py  # noqa: PLC0415
+
+    ctx.contract_rows(n, use_graph=1)  # records and captures
+    walls, devs, r = [], [], None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r = ctx.contract_rows(n, use_graph=1)
+        walls.append(time.perf_counter() - t0)
+        devs.append(r.device["device_ms"] / 1e3)
+        assert r.count == pkg.known_count(n)
+    entries = r.device["entries_in"] if r.device["batches"] == 1 else None
+    oracle_py.build()
+    cw = []
+    for _ in range(cpu_repeats):
+        t0 = time.perf_counter()
+        o = oracle_py.contract(n, backend=oracle_py.PARALLEL_SORT_REDUCE, threads=threads)
+        cw.append(time.perf_counter() - t0)
+        assert o["count"] == pkg.known_count(n)
+    cpu_entries = sum(l["input_states"] for l in o["layers"] if l["row"] >= 1)
+    gw, gd, cm = statistics.median(walls), statistics.median(devs), statistics.median(cw)
+    return {
+        "workload": f"Q({n}) exact, all first-row orbit slices, full contraction on both sides",
+        "count": str(r.count),
+        "gpu_wall_s": gw,
+        "gpu_device_s": gd,
+        "cpu_wall_s": cm,
+        "cpu_wall_s_all": cw,
+        "cpu_threads": threads,
+        "cpu_kind": "threaded C++ restatement of contract_rows_d4_orbit_parallel_sort_reduce (src/lib.rs:5469-5626)",
+        "boundary_entries": entries,
+        "cpu_boundary_entries": cpu_entries,
+        "gpu_entries_per_s": (entries / gw) if entries else None,
+        "cpu_entries_per_s": cpu_entries / cm,
+        "wall_speedup": cm / gw,
+    }
 
 
 def run_ours(args):
@@ -210,7 +285,7 @@ def run_ours(args):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    ctx = pkg.Context(local if world > 1 else 0)
+    device = local if world > 1 else 0
     opts = {"use_graph": 0 if args.no_graph else 1}
     if args.slice_depth:
         opts["slice_depth"] = args.slice_depth
@@ -218,6 +293,11 @@ def run_ours(args):
         opts["granularity"] = pkg.GRAIN_SITE
     if args.tail_row is not None:
         opts["tail_row"] = args.tail_row
+    merged = merged_entries(pkg, args.n, device, opts) if args.grain == "row" else None
+    ctx = pkg.Context(device)
+    tuning_note = None
+    if args.tuning_cache and Path(args.tuning_cache).exists():
+        tuning_note = ctx.load_tuning(args.n, Path(args.tuning_cache))
 
     def barrier():
         if world > 1:
@@ -229,7 +309,7 @@ def run_ours(args):
         r = ctx.contract_rows(args.n, **opts)
         assert r.count == pkg.known_count(args.n)
     barrier()
-    sampler = ClockSampler(local if world > 1 else 0)
+    sampler = ClockSampler(device)
     sampler.start()
     results, walls = [], []
     t_all0 = time.perf_counter()
@@ -244,8 +324,14 @@ def run_ours(args):
     barrier()
     clocks = sampler.stop()
 
-    entries_run = results[-1].device["entries_in"]
-    entries = MERGED_ENTRIES.get(args.n, entries_run) if results[-1].device["batches"] > 1 else entries_run
+    d = results[-1].device
+    entries_run = d["entries_in"]
+    if d["batches"] == 1:
+        entries, entries_kind = entries_run, "merged (one device batch)"
+    elif merged is not None:
+        entries, entries_kind = merged, "merged (measured in this run, one untimed single-batch contraction)"
+    else:
+        entries, entries_kind = entries_run, "processed (the merged figure could not be measured)"
     dev_s = max(sum(x.device["device_ms"] for x in results) / len(results) / 1e3, 1e-12)
     wall_s = max(t_all / args.steps, 1e-12)
     if world > 1:
@@ -256,25 +342,32 @@ def run_ours(args):
     e2e = entries * world / wall_s
 
     peak, peak_kind = measured_peaks()
-    d = results[-1].device
     achieved = d["merge_kernel_bytes"] / max(d["device_ms"] / 1e3, 1e-12) / 1e9
+    tuning = ctx.tuning
+    kind = tuning.get("scatter_kind")
+    tpb = TRAFFIC_PER_ALGORITHMIC_BYTE.get(kind) if d["merge"] == 2 and args.grain == "row" else None
     roofline = {
         "bound": "hbm",
-        "kernel": ("merge step: partition_scatter_list_kernel + partition_merge_list_kernel" if d["merge"] == 2
+        "kernel": ("merge step: partition scatter + partition merge kernels" if d["merge"] == 2
                    else "merge step: row_expand_insert_kernel + compact_kernel (global table)"),
         "achieved": achieved,
         "peak": peak,
         "peak_kind": peak_kind,
         "unit": "GB/s",
         "frac": achieved / peak,
-        "traffic": (DRAM_TRAFFIC_PER_STEP.get(args.n) if d["merge"] == 2 and args.grain == "row" else None),
-        "traffic_scope": "DRAM bytes per step (one contraction), ncu, all scatter + merge launches",
+        "traffic": (tpb * d["merge_kernel_bytes"]) if tpb else None,
+        "traffic_scope": ("DRAM bytes per step, scaled from the DRAM bytes per algorithmic byte of an ncu capture of "
+                          "peak-row scatter and merge launches" if tpb else "no capture for this configuration"),
         "algorithmic_bytes_per_step": d["merge_kernel_bytes"],
         "launches_per_step": d["merge_kernel_launches"],
         "scatter_ms_per_step": d["scatter_kernel_ms"],
         "merge_ms_per_step": d["merge_kernel_ms"],
         "step_ms_per_step": d["device_ms"],
     }
+    if d["exact_weights"]:
+        dtype = f"u{d['key_bits']} keys + exact u64 weights (2x u32 words), host-side CRT bookkeeping"
+    else:
+        dtype = f"u{d['key_bits']} keys + {d['residues']}x u32 residues"
     line = {
         "metric": METRIC,
         "value": value,
@@ -286,25 +379,25 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": f"u{d['key_bits']} keys + {d['residues']}x u32 residues",
+        "dtype": dtype,
         "data": "synthetic (empty N x N board; the workload has no external input)",
-        "config": {
-            "workload": f"Q({args.n}) exact, all first-row orbit slices",
-            "n": args.n,
-            "grain": args.grain,
+        "config": workload_config(args),
+        "run": {
             "slice_depth": d["slice_depth"],
             "batches": d["batches"],
             "residues": d["residues"],
+            "exact_weights": bool(d["exact_weights"]),
             "key_bits": d["key_bits"],
             "merge": {1: "hash", 2: "partition"}.get(d["merge"], d["merge"]),
-            "l2": "inputs larger than L2 (boundary buffers of GBs per row)",
-            "parallelism": "replicas" if world > 1 else "single",
             "cuda_graph": not args.no_graph,
+            "tuning": tuning,
+            "tuning_cache": tuning_note,
         },
         "count": str(results[-1].count),
         "wall_s_per_step": wall_s,
         "device_s_per_step": dev_s,
         "boundary_entries_per_step": entries,
+        "boundary_entries_kind": entries_kind,
         "boundary_entries_processed_per_step": entries_run,
         "peak_states": results[-1].peak_states,
         "peak_device_bytes": d["peak_device_bytes"],
@@ -316,37 +409,44 @@ def run_ours(args):
     }
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        ce, cw, _ = cpu_sample(args.n, args.cpu_rows, threads)
+        samples = [cpu_sample(args.n, args.cpu_rows, threads)[:2] for _ in range(3)]
+        rates = [e / w for e, w in samples]
         line["cpu_baseline"] = {
-            "value": ce / cw, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {args.cpu_rows} rows of Q({args.n}) ({ce} boundary entries), threaded C++ "
-                      f"restatement of contract_rows_d4_orbit_parallel_sort_reduce",
+            "value": statistics.median(rates), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {args.cpu_rows} rows of Q({args.n}) ({samples[0][0]} boundary entries), threaded C++ "
+                      f"restatement of contract_rows_d4_orbit_parallel_sort_reduce (src/lib.rs:5469-5626); "
+                      f"median of 3 samples",
+            "samples": rates,
         }
-    print(json.dumps(line), flush=True)
+        if args.same_workload_n:
+            line["same_workload"] = same_workload_pair(pkg, ctx, args.same_workload_n, threads)
     ctx.close()
+    if world == 1 and args.serve_requests_inline:
+        line["serve"] = serve_stream(pkg, args, requests=args.serve_requests_inline, check_nmax=13,
+                                     sample_per_n=0, alone_samples=16, compact=True)
+    print(json.dumps(line), flush=True)
 
 
-def run_serve(args):
-    """Seeded Poisson stream of counting requests through the continuous-batching
-    server. Prints one JSON line: p50/p99 latency and requests/s."""
+def serve_stream(pkg, args, requests: int, check_nmax: int, sample_per_n: int, alone_samples: int,
+                 compact: bool = False) -> dict:
+    """Seeded Poisson stream of counting requests through the
+    continuous-batching server; latency percentiles, throughput and exactness
+    checks (after the timed stream)."""
     import random  # noqa: PLC0415
 
-    world, rank, _ = dist_env()
-    if rank != 0:
-        return
-    pkg = importlib.import_module(PACKAGE)
-    if not pkg.LIBRARY_PATH.exists():
-        pkg.build()
     rng = random.Random(args.serve_seed)
     reqs = []
     t = 0.0
-    for tag in range(args.serve_requests):
+    for tag in range(requests):
         t += rng.expovariate(args.serve_rate)
         n = rng.randint(args.serve_nmin, args.serve_nmax)
         k = rng.randint(0, 3)
         reqs.append((t, tag, n, pkg.random_prefix(rng, n, k)))
     got = {}
-    sv = pkg.Server(0, use_cache=int(not args.serve_no_cache))
+    cfg = {"use_cache": int(not args.serve_no_cache)}
+    if args.serve_large_workers:
+        cfg["large_workers"] = args.serve_large_workers
+    sv = pkg.Server(0, **cfg)
     sampler = ClockSampler(0)
     sampler.start()
     t0 = time.perf_counter()
@@ -368,11 +468,11 @@ def run_serve(args):
     sv.close()
     lat = sorted(c["latency_s"] for c in got.values())
     q = lambda xs, f: xs[min(len(xs) - 1, int(f * len(xs)))] if xs else None  # noqa: E731
-    computed = sorted(c["latency_s"] for c in got.values() if c["path"] != "cache")
-    # Exactness (after the timed stream): k = 0 against the known counts; every
-    # distinct request with N <= serve_check_nmax against the CPU oracle; a
-    # seeded sample of larger boards against the oracle; a sample recomputed
-    # alone through a fresh context; the sum rule over all 1-row prefixes.
+    computed = sorted(c["latency_s"] for c in got.values() if c["path"] not in ("cache", "coalesced"))
+    # Exactness: k = 0 against the known counts; every distinct request with
+    # N <= check_nmax against the CPU oracle; a seeded sample of larger boards
+    # against the oracle; a sample recomputed alone through a fresh context;
+    # the sum rule over all 1-row prefixes.
     import oracle_py  # noqa: PLC0415
 
     oracle_py.build()
@@ -393,7 +493,7 @@ def run_serve(args):
         if key not in want:
             if not prefix:
                 want[key] = pkg.known_count(n)
-            elif n <= args.serve_check_nmax:
+            elif n <= check_nmax:
                 want[key] = oracle_count(n, prefix)
             else:
                 big.append((tag, key))
@@ -408,7 +508,7 @@ def run_serve(args):
     for n in sorted(by_n):
         pool = sorted(by_n[n], key=lambda tk: -len(tk[1][1]))  # deepest prefixes first: smallest frontiers
         deep = [tk for tk in pool if len(tk[1][1]) == len(pool[0][1][1])]
-        for tag, key in srng.sample(deep, min(args.serve_sample_per_n, len(deep))):
+        for tag, key in srng.sample(deep, min(sample_per_n, len(deep))):
             if key not in want:
                 want[key] = oracle_count(*key)
             checked += 1
@@ -416,27 +516,25 @@ def run_serve(args):
             wrong += int(got[tag]["count"] != want[key] or got[tag]["status"] != 0)
     alone_checked = alone_wrong = 0
     ctx = pkg.Context(0)
-    for _, tag, n, prefix in srng.sample(reqs, min(64, len(reqs))):
+    for _, tag, n, prefix in srng.sample(reqs, min(alone_samples, len(reqs))):
         if tag in got and n <= 17:
             alone_checked += 1
             alone_wrong += int(ctx.count(n, prefix) != got[tag]["count"])
     n_rule = min(args.serve_nmax, 16)
     rule_sum = sum(ctx.count(n_rule, [c]) for c in range(n_rule))
     ctx.close()
-    sum_rule_ok = rule_sum == pkg.known_count(n_rule)
     paths = {}
     for c in got.values():
         paths[c["path"]] = paths.get(c["path"], 0) + 1
-    line = {
+    out = {
         "metric": "serve p50/p99 latency (mixed-N prefix counting stream)",
         "value": len(got) / wall,
         "unit": "requests/s",
-        "n_gpus": 1,
-        "higher_is_better": True,
-        "p50_latency_s": q(lat, 0.50),
-        "p99_latency_s": q(lat, 0.99),
         "computed_p50_latency_s": q(computed, 0.50),
         "computed_p99_latency_s": q(computed, 0.99),
+        "computed_requests": len(computed),
+        "p50_latency_s": q(lat, 0.50),
+        "p99_latency_s": q(lat, 0.99),
         "completed": len(got),
         "submitted": len(reqs),
         "wall_s": wall,
@@ -444,15 +542,32 @@ def run_serve(args):
         "wrong": wrong,
         "checked_large_sample": sampled,
         "alone_vs_mixed": {"checked": alone_checked, "wrong": alone_wrong},
-        "sum_rule": {"n": n_rule, "ok": sum_rule_ok},
+        "sum_rule": {"n": n_rule, "ok": rule_sum == pkg.known_count(n_rule)},
         "paths": paths,
         "server": stats,
-        "clocks": clocks,
         "config": {"workload": "Poisson stream, N ~ U{%d..%d}, k ~ U{0..3} random legal prefixes"
-                   % (args.serve_nmin, args.serve_nmax), "requests": args.serve_requests,
-                   "rate_per_s": args.serve_rate, "seed": args.serve_seed, "cache": not args.serve_no_cache},
-        "data": "synthetic (seeded request stream)",
+                   % (args.serve_nmin, args.serve_nmax), "requests": requests,
+                   "rate_per_s": args.serve_rate, "seed": args.serve_seed, "cache": not args.serve_no_cache,
+                   "large_workers": args.serve_large_workers or "default"},
     }
+    if not compact:
+        out["clocks"] = clocks
+        out["n_gpus"] = 1
+        out["higher_is_better"] = True
+        out["data"] = "synthetic (seeded request stream)"
+    return out
+
+
+def run_serve(args):
+    """The full serving stream; one JSON line."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = importlib.import_module(PACKAGE)
+    if not pkg.LIBRARY_PATH.exists():
+        pkg.build()
+    line = serve_stream(pkg, args, requests=args.serve_requests, check_nmax=args.serve_check_nmax,
+                        sample_per_n=args.serve_sample_per_n, alone_samples=64)
     print(json.dumps(line), flush=True)
 
 
@@ -469,16 +584,24 @@ def main():
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--same-workload-n", type=int, default=16,
+                    help="full Q(n) on both the GPU and the CPU oracle beside the headline (0: skip)")
+    ap.add_argument("--tuning-cache", default=str(ROOT / "profiles" / "tuning_gb300.json"),
+                    help="autotuner cache (JSON) whose entry for this device and N is applied before timing")
     ap.add_argument("--no-graph", action="store_true",
                     help="contract eagerly every step (default: the first warm-up step captures the row steps "
                          "as a CUDA graph and later steps replay it)")
     ap.add_argument("--serve", action="store_true", help="run the serving stream instead of the Q(N) step")
     ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-requests-inline", type=int, default=1000,
+                    help="requests of the short stream reported in the default line (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
     ap.add_argument("--serve-seed", type=int, default=20261203)
     ap.add_argument("--serve-nmin", type=int, default=10)
     ap.add_argument("--serve-nmax", type=int, default=19)
     ap.add_argument("--serve-no-cache", action="store_true")
+    ap.add_argument("--serve-large-workers", type=int, default=0,
+                    help="concurrent large-request contexts of the server (0: library default)")
     ap.add_argument("--serve-check-nmax", type=int, default=15)
     ap.add_argument("--serve-sample-per-n", type=int, default=2, help="oracle-checked requests per N above the check limit")
     ap.add_argument("--serve-timeout", type=float, default=900.0)

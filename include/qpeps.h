@@ -91,7 +91,8 @@ typedef struct qpeps_result {
   uint64_t merge_kernel_launches;
   uint64_t merge_kernel_bytes; /* algorithmic bytes of the dominant kernel */
   uint32_t tail_row;          /* first row contracted by the slice-tail kernel (N = none) */
-  uint32_t pad0;
+  uint32_t exact_weights;     /* 1: the boundary's two u32 planes held each entry's exact 64-bit weight
+                                 (low and high words) and the host derived the residues; 0: residue planes */
   uint64_t tail_items;        /* boundary entries handed to the slice-tail kernel */
   uint64_t tail_overflow;     /* of those, entries redone by the row engine */
   double tail_kernel_ms;      /* device time of the slice-tail kernel */

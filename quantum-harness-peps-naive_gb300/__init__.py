@@ -99,7 +99,7 @@ class Result(ctypes.Structure):
         ("merge_kernel_launches", ctypes.c_uint64),
         ("merge_kernel_bytes", ctypes.c_uint64),
         ("tail_row", ctypes.c_uint32),
-        ("pad0", ctypes.c_uint32),
+        ("exact_weights", ctypes.c_uint32),
         ("tail_items", ctypes.c_uint64),
         ("tail_overflow", ctypes.c_uint64),
         ("tail_kernel_ms", ctypes.c_double),
@@ -383,6 +383,7 @@ def _result_from(res: Result, layers: Sequence[Layer] | None) -> ContractionResu
         "merge_kernel_launches": res.merge_kernel_launches,
         "merge_kernel_bytes": res.merge_kernel_bytes,
         "tail_row": res.tail_row,
+        "exact_weights": res.exact_weights,
         "tail_items": res.tail_items,
         "tail_overflow": res.tail_overflow,
         "tail_kernel_ms": res.tail_kernel_ms,
@@ -536,6 +537,26 @@ class Context:
         library().qpeps_ctx_device_name(self._h, buf, len(buf))
         return buf.value.decode(errors="replace")
 
+    def tuning_key(self, n: int) -> str:
+        """Autotuner cache key: device name, library version and probe size."""
+        return f"{self.device_name}|{version()}|n={int(n)}"
+
+    def load_tuning(self, n: int, cache: str | Path) -> dict | None:
+        """Apply the cached autotuner result for this device, library version
+        and ``n`` (no search); returns the cache entry, or None when the cache
+        holds none."""
+        import json
+
+        try:
+            entries = json.loads(Path(cache).read_text())
+        except (OSError, ValueError):
+            return None
+        e = entries.get(self.tuning_key(n))
+        if e is None:
+            return None
+        self.set_tuning(**e["tuning"])
+        return {"key": self.tuning_key(n), **e}
+
     def autotune(self, n: int = 16, repeats: int = 2, cache: str | Path | None = None) -> dict:
         """Pick the fastest tuning for this device (``qpeps_autotune`` on a
         probe contraction of size ``n``). With ``cache``, a JSON file keyed
@@ -544,7 +565,7 @@ class Context:
         "cached": bool}``."""
         import json
 
-        key = f"{self.device_name}|{version()}|n={int(n)}"
+        key = self.tuning_key(n)
         path = Path(cache) if cache is not None else None
         entries = {}
         if path is not None and path.exists():

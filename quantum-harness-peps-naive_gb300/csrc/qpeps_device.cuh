@@ -127,6 +127,33 @@ __host__ __device__ __forceinline__ K row_successor(const State& s, u64 bit, uns
   return pack<K>(s.cols | bit, ((s.dr | bit) << 1) & mask, (s.dl | bit) >> 1, n);
 }
 
+// C entries matched by the reference's per-parent sitewise row kernel
+// (contract_one_row_sitewise, src/lib.rs:513-592, counters at 538-541) for a
+// parent whose free columns are `fr`: the partial row that has placed no queen
+// yet matches two entries at a free column (pass through or place) and one
+// elsewhere; every partial that has placed its queen matches one entry per
+// later column. Summed over the n columns: n + f + sum over free b of
+// (n - 1 - b) = n + f * n - (sum of the free column indices), f = popcount.
+__host__ __device__ __forceinline__ u64 sitewise_entries(u64 fr, unsigned n) {
+  u64 idx_sum = 0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const u64 m = j == 0 ? 0xAAAAAAAAAAAAAAAAull : j == 1 ? 0xCCCCCCCCCCCCCCCCull : j == 2 ? 0xF0F0F0F0F0F0F0F0ull
+                : j == 3 ? 0xFF00FF00FF00FF00ull : j == 4 ? 0xFFFF0000FFFF0000ull : 0xFFFFFFFF00000000ull;
+#if defined(__CUDA_ARCH__)
+    idx_sum += (u64)__popcll(fr & m) << j;
+#else
+    idx_sum += (u64)__builtin_popcountll(fr & m) << j;
+#endif
+  }
+#if defined(__CUDA_ARCH__)
+  const u64 f = (u64)__popcll(fr);
+#else
+  const u64 f = (u64)__builtin_popcountll(fr);
+#endif
+  return (u64)n + f * n - idx_sum;
+}
+
 // ---- key layouts of the partitioned merge ----------------------------------
 //
 // FixedLayout: one board size, the reference's PackedBoundary bit layout.

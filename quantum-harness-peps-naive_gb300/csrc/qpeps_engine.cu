@@ -890,11 +890,16 @@ static void run_chunks(Ctx& ctx, const Plan& p, std::vector<HostChunk> pending, 
       StepOut so;
       if (p.grain == QPEPS_GRAIN_SITE) {
         if (!counted) {
+          // The sitewise backend's counters: C entries matched per parent
+          // (counted on the device from the row's input keys), no row
+          // operator counts.
           const u64 row_terms = count_terms(ctx, p, f, false, 0, rs);
           acc.input_states += f.count;
-          acc.candidates += (u128)f.count * p.n;
-          acc.matched += row_terms;
           acc.completed += row_terms;
+          if (f.count) {  // count_terms ran the count kernel
+            acc.examined += ctx.h_sc->sitewise_examined;
+            acc.tmatched += ctx.h_sc->sitewise_examined;
+          }
         }
         for (unsigned site = site0; site < p.n; ++site) {
           const bool fin = last_row && site + 1 == p.n;
@@ -935,7 +940,11 @@ static void run_chunks(Ctx& ctx, const Plan& p, std::vector<HostChunk> pending, 
 // Host expansion of one row over a merged item list (used for the first
 // row(s) that seed slices): compiled successor + optional orbit weights,
 // merged by key (checked u128).
-static std::vector<Item> host_expand(unsigned n, const std::vector<Item>& in, unsigned row, bool orbit, RowAcc& acc) {
+// With `sitewise` (site granularity) the row's counters are those of the
+// reference's sitewise backend: C entries matched per parent, and no row
+// operator counts (src/lib.rs:5633-5750).
+static std::vector<Item> host_expand(unsigned n, const std::vector<Item>& in, unsigned row, bool orbit, RowAcc& acc,
+                                     bool sitewise) {
   const u64 mask = (n >= 64) ? ~0ull : ((1ull << n) - 1);
   std::map<u128, u128> next;
   acc.used = true;
@@ -943,11 +952,16 @@ static std::vector<Item> host_expand(unsigned n, const std::vector<Item>& in, un
   for (const Item& it : in) {
     State s = unpack<u128>(it.key, n, mask);
     u64 fr = ~(s.cols | s.dr | s.dl) & mask;
-    acc.candidates += n;
+    if (sitewise) {
+      acc.examined += sitewise_entries(fr, n);
+      acc.tmatched += sitewise_entries(fr, n);
+    } else {
+      acc.candidates += n;
+    }
     while (fr) {
       const u64 b = fr & (~fr + 1);
       fr &= fr - 1;
-      acc.matched += 1;
+      if (!sitewise) acc.matched += 1;
       u128 w = it.weight;
       if (row == 0 && orbit) {
         const unsigned c = (unsigned)__builtin_ctzll(b), mirror = n - 1 - c;
@@ -1589,7 +1603,7 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
   const unsigned depth = std::max<unsigned>(o.slice_depth ? o.slice_depth : 1, row0 == 0 ? 1 : row0);
   while (row0 < depth && row0 < n) {
     RowAcc& acc = out.rows[row0];
-    items = host_expand(n, items, row0, orbit && row0 == 0, acc);
+    items = host_expand(n, items, row0, orbit && row0 == 0, acc, out.plan.grain == QPEPS_GRAIN_SITE);
     acc.device_row = false;
     out.peak_states = std::max<u64>(out.peak_states, items.size());
     ++row0;
@@ -1618,7 +1632,7 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
         break;
       }
       RowAcc& acc = out.rows[row0];
-      items = host_expand(n, items, row0, false, acc);
+      items = host_expand(n, items, row0, false, acc, out.plan.grain == QPEPS_GRAIN_SITE);
       acc.device_row = false;
       ++row0;
     }
@@ -1676,8 +1690,16 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
     ++nl;
   }
   r->n_layers = nl;
-  r->tensor_entries_examined = to_abi(n ? 17 : 0);
-  r->tensor_entries_matched = to_abi(n ? 17 : 0);
+  // The compiled row operator examines the 17 C entries once (src/lib.rs:5654-5655);
+  // the sitewise backend reports the entries its per-parent site kernel matched.
+  u128 examined = 0, tmatched = 0;
+  for (const RowAcc& a : c.rows) {
+    examined += a.examined;
+    tmatched += a.tmatched;
+  }
+  const bool sitewise = n && c.plan.grain == QPEPS_GRAIN_SITE;
+  r->tensor_entries_examined = to_abi(sitewise ? examined : (n ? 17 : 0));
+  r->tensor_entries_matched = to_abi(sitewise ? tmatched : (n ? 17 : 0));
   r->row_operator_candidates = to_abi(cand);
   r->row_operator_matched = to_abi(matched);
   r->peak_rss_bytes = ctx.peak_pool_bytes;
@@ -1697,6 +1719,7 @@ static void fill_result(const Ctx& ctx, const Contraction& c, unsigned n, qpeps_
   r->merge_kernel_launches = c.rs.merge_launches;
   r->merge_kernel_bytes = c.rs.merge_bytes;
   r->tail_row = n ? c.plan.tail_row : 0;
+  r->exact_weights = (n && c.plan.w64) ? 1u : 0u;
   r->tail_items = c.rs.tail_items;
   r->tail_overflow = c.rs.tail_overflow;
   r->tail_kernel_ms = c.rs.tail_ms;

@@ -82,13 +82,17 @@ template <typename K, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) row_count_kernel(const void* __restrict__ keys, u64 n_in, unsigned n,
                                                           StepScalars* __restrict__ sc) {
   const u64 mask = board_mask(n);
-  unsigned long long acc = 0;
+  unsigned long long acc = 0, sw = 0;
   for (u64 i = (u64)blockIdx.x * BLOCK + threadIdx.x; i < n_in; i += (u64)gridDim.x * BLOCK) {
     State s = unpack<K>(load_key<K>(keys, i), n, mask);
-    acc += __popcll(~(s.cols | s.dr | s.dl) & mask);
+    const u64 fr = ~(s.cols | s.dr | s.dl) & mask;
+    acc += __popcll(fr);
+    sw += sitewise_entries(fr, n);
   }
   unsigned long long t = block_sum_u64<BLOCK>(acc);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->terms, t);
+  t = block_sum_u64<BLOCK>(sw);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->sitewise_examined, t);
 }
 
 // ---------------------------------------------------------------------------

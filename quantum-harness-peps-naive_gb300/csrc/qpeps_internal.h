@@ -34,7 +34,10 @@ struct StepScalars {
   unsigned long long final_sum[4];   // sum of residues of entries with all columns set
   unsigned long long final_states;   // entries with all columns set
   unsigned int error;                // ErrorBits
-  unsigned int pad[7];
+  unsigned int pad0;
+  unsigned long long sitewise_examined;  // row count: C entries the reference's per-parent sitewise
+                                         // row kernel matches over the input (sitewise_entries())
+  unsigned int pad[4];
 };
 
 struct LaunchCfg {

@@ -12,13 +12,17 @@
 // library holds kNoAllocScratchBytes (48 MiB) of device memory until the
 // process exits. Host code cannot use the array's name as a device address:
 // the first call on each device looks the address up with
-// cudaGetSymbolAddress (with that device current) and caches it, so make that
-// first call before any stream capture. All calls share the array and it keeps
-// the previous call's contents, so each call clears the cursors and scalars it
-// uses; calls whose GPU work overlaps (different streams or threads) race on
-// it and must be serialised by the caller.
+// cudaGetSymbolAddress (with that device current) and caches it beside the
+// CUDA context that was current, so make that first call before any stream
+// capture. A call made under a different context of the same device (after a
+// device reset, or from a non-primary driver context) looks the address up
+// again. All calls share the array and it keeps the previous call's contents,
+// so each call clears the cursors and scalars it uses; calls whose GPU work
+// overlaps (different streams or threads) race on it and must be serialised
+// by the caller.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -38,6 +42,24 @@ static __device__ __align__(256) unsigned char g_step_scratch[kNoAllocScratchByt
 
 std::mutex g_addr_mutex;
 void* g_addr[kMaxDevices] = {nullptr};
+void* g_addr_ctx[kMaxDevices] = {nullptr};  // CUDA context current when g_addr[dev] was looked up
+
+// The CUDA context current on this thread (driver cuCtxGetCurrent, fetched
+// through the runtime so the library does not link libcuda), or null.
+void* current_context() {
+  using GetCurrent = int (*)(void**);
+  static GetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<GetCurrent>(f);
+  }();
+  void* c = nullptr;
+  if (!fn || fn(&c) != 0) return nullptr;
+  return c;
+}
 
 int set_err(char* err, size_t len, int code, const char* msg) {
   if (err && len) std::snprintf(err, len, "%s", msg);
@@ -65,7 +87,8 @@ extern "C" int qpeps_row_step_noalloc(uint32_t n, uint32_t residues, const uint6
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[dev]) {
+    void* ctx = current_context();
+    if (!g_addr[dev] || ctx != g_addr_ctx[dev]) {
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_step_scratch);
       if (e != cudaSuccess || !p) {
@@ -73,6 +96,7 @@ extern "C" int qpeps_row_step_noalloc(uint32_t n, uint32_t residues, const uint6
         return set_err(err, err_len, QPEPS_ERR_CUDA, buf);
       }
       g_addr[dev] = p;
+      g_addr_ctx[dev] = current_context();  // the lookup makes the primary context current if none was
     }
     base = g_addr[dev];
   }
@@ -116,20 +140,29 @@ extern "C" int qpeps_row_step_noalloc(uint32_t n, uint32_t residues, const uint6
     return set_err(err, err_len, QPEPS_ERR_CAPACITY, buf);
   }
   if (terms > 0) {
-    const uint32_t parts = (uint32_t)std::min<uint64_t>(max_parts, (uint64_t)((double)terms / kNoAllocMean) + 1);
-    PartitionCfg pc{(int)residues, sms, parts, cap, residues == 1 ? 3 : residues == 2 ? 2 : 1};
-    FrontierView out{keys_out, res_out, out_cap};
-    e = cudaMemsetAsync(cursors, 0, (size_t)parts * 4, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_sc, 0, sizeof(StepScalars), st);
-    if (e == cudaSuccess) e = launch_partition_scatter(pc, in, n_in, n, regions, cursors, d_sc, st);
-    if (e == cudaSuccess) e = launch_partition_merge(pc, regions, cursors, out, n, true, d_sc, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-      std::snprintf(buf, sizeof buf, "row step: %s", cudaGetErrorString(e));
-      return set_err(err, err_len, QPEPS_ERR_CUDA, buf);
+    // A partition that overflows (hash skew) makes the merge write nothing,
+    // so the input is intact and the step can run again with more, emptier
+    // partitions while the scratch holds them.
+    double mean = kNoAllocMean;
+    for (int attempt = 0;; ++attempt) {
+      const uint32_t parts = (uint32_t)std::min<uint64_t>(max_parts, (uint64_t)((double)terms / mean) + 1);
+      PartitionCfg pc{(int)residues, sms, parts, cap, residues == 1 ? 3 : residues == 2 ? 2 : 1};
+      FrontierView out{keys_out, res_out, out_cap};
+      e = cudaMemsetAsync(cursors, 0, (size_t)parts * 4, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(d_sc, 0, sizeof(StepScalars), st);
+      if (e == cudaSuccess) e = launch_partition_scatter(pc, in, n_in, n, regions, cursors, d_sc, st);
+      if (e == cudaSuccess) e = launch_partition_merge(pc, regions, cursors, out, n, true, d_sc, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        std::snprintf(buf, sizeof buf, "row step: %s", cudaGetErrorString(e));
+        return set_err(err, err_len, QPEPS_ERR_CUDA, buf);
+      }
+      if (!h.error) break;
+      if (attempt >= 3 || parts >= max_parts)
+        return set_err(err, err_len, QPEPS_ERR_CAPACITY, "a hash partition overflowed its slots");
+      mean *= 0.75;
     }
-    if (h.error) return set_err(err, err_len, QPEPS_ERR_CAPACITY, "a hash partition overflowed its slots");
   } else {
     std::memset(&h, 0, sizeof h);
   }

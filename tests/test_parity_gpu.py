@@ -90,6 +90,45 @@ def test_site_grain_equals_row_grain(ctx, n):
         (l.input_states, l.output_states, l.output_weight, l.completed_row_terms) for l in r.layers]
 
 
+SITEWISE_FIELDS = ["row", "input_states", "tensor_entries_examined", "tensor_entries_matched",
+                   "row_operator_candidates", "row_operator_matched", "completed_row_terms", "output_states",
+                   "output_weight"]
+
+
+@pytest.mark.parametrize("n", range(1, 11))
+def test_site_grain_counters_match_sitewise_backend(ctx, oracle, n):
+    # The plain per-site form is the reference's sitewise backend
+    # (contract_rows_with_backend(Sitewise), src/lib.rs:5633-5750): per row the
+    # C entries its per-parent site kernel matched (src/lib.rs:538-541), no
+    # row-operator counts, and the same frontier, against the oracle's HashMap
+    # sitewise driver on the dense (no symmetry) board.
+    g = ctx.contract_rows(n, granularity=1, symmetry=0)
+    o = oracle.contract(n, backend=O.HASH_SITEWISE, symmetry=False)
+    assert g.count == o["count"] == oracle.known_count(n)
+    assert [tuple(getattr(l, f) for f in SITEWISE_FIELDS) for l in g.layers] == [
+        tuple(l[f] for f in SITEWISE_FIELDS) for l in o["layers"]]
+    assert (g.tensor_entries_examined, g.tensor_entries_matched) == (o["tensor_entries_examined"],
+                                                                    o["tensor_entries_matched"])
+    assert (g.row_operator_candidates, g.row_operator_matched) == (0, 0) == (o["row_operator_candidates"],
+                                                                             o["row_operator_matched"])
+    assert g.peak_states == o["peak_states"]
+
+
+def test_site_grain_n16_plain_form(ctx, qp, golden):
+    # Config 2: one plain launch per site over the whole N=16 board; every row
+    # equals the batched row form (whose N=16 peak and matched work equal the
+    # published benchmarks/e36_joint_u64_release.csv values).
+    s = ctx.contract_rows(16, granularity=1)
+    r = ctx.contract_rows(16)
+    assert s.count == r.count == 14772512 == golden["e36_orbit_n16"]["16"]["count"]
+    assert s.device["merge"] == qp.MERGE_HASH
+    assert [(l.input_states, l.completed_row_terms, l.output_states, l.output_weight) for l in s.layers] == [
+        (l.input_states, l.completed_row_terms, l.output_states, l.output_weight) for l in r.layers]
+    assert max(l.output_states for l in r.layers) == golden["e36_orbit_n16"]["16"]["peak_support"]
+    # 16 x 16 site launches plus the row counts, against 2 or 3 launches per row
+    assert s.device["gpu_launches"] > 16 * 15 and r.device["gpu_launches"] < 3 * 16
+
+
 @pytest.mark.parametrize("n", [1, 4, 8, 11, 12])
 def test_forced_wide_keys_are_exact(ctx, oracle, n):
     g = ctx.contract_rows(n, key_bits=128)
