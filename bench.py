@@ -298,6 +298,9 @@ def run_ours(args):
     tuning_note = None
     if args.tuning_cache and Path(args.tuning_cache).exists():
         tuning_note = ctx.load_tuning(args.n, Path(args.tuning_cache))
+    if args.set_tuning:
+        kv = dict(item.split("=", 1) for item in args.set_tuning.split(","))
+        ctx.set_tuning(**{k: (float(v) if "." in v else int(v)) for k, v in kv.items()})
 
     def barrier():
         if world > 1:
@@ -588,6 +591,8 @@ def main():
                     help="full Q(n) on both the GPU and the CPU oracle beside the headline (0: skip)")
     ap.add_argument("--tuning-cache", default=str(ROOT / "profiles" / "tuning_gb300.json"),
                     help="autotuner cache (JSON) whose entry for this device and N is applied before timing")
+    ap.add_argument("--set-tuning", default="",
+                    help="tuning fields applied before timing, e.g. scatter_kind=3,unit_target=1000")
     ap.add_argument("--no-graph", action="store_true",
                     help="contract eagerly every step (default: the first warm-up step captures the row steps "
                          "as a CUDA graph and later steps replay it)")

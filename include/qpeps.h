@@ -215,6 +215,10 @@ int qpeps_explicit_frontier(void* ctx, uint32_t n, uint32_t order, uint64_t supp
                                      shared memory (16-byte candidates, up to 2^20 partitions; the
                                      window scatter elsewhere); needs about one more candidate array;
                                      exact like the others, measured slower on GB300 */
+#define QPEPS_SCATTER_CLASS 3  /* class-grouped partitions: a candidate's partition follows its columns
+                                  and outermost diagonal signals, so a CTA's successors go to few
+                                  partitions and are written as runs (16-byte candidates; the window
+                                  scatter elsewhere) */
 #define QPEPS_MERGEK_SCAN 0    /* ballot/scan compaction over the whole table */
 #define QPEPS_MERGEK_CLAIM 1   /* claim list + first-claimant stores (default) */
 
@@ -234,6 +238,9 @@ typedef struct qpeps_tuning {
                                     per key; 0 = residue sums throughout */
   double partition_fill;         /* mean candidates per partition / capacity, in [0.3, 0.95] */
   double slice_margin;           /* predictive slicing: assumed slice peak / mean slice peak, >= 1 */
+  uint32_t unit_target;          /* QPEPS_SCATTER_CLASS: planned candidates per partition, 256..2048 */
+  uint32_t unit_sample;          /* QPEPS_SCATTER_CLASS: 1 in unit_sample parents sampled for the plan
+                                    (a power of two, 1..64) */
 } qpeps_tuning;
 
 /* Library defaults (what a new context starts with). */

@@ -43,6 +43,7 @@ MERGE_PARTITION = 2
 SCATTER_SEARCH = 0
 SCATTER_WINDOW = 1
 SCATTER_TWO_LEVEL = 2
+SCATTER_CLASS = 3
 MERGEK_SCAN = 0
 MERGEK_CLAIM = 1
 
@@ -194,6 +195,8 @@ class Tuning(ctypes.Structure):
         ("fold_weights", ctypes.c_uint32),
         ("partition_fill", ctypes.c_double),
         ("slice_margin", ctypes.c_double),
+        ("unit_target", ctypes.c_uint32),
+        ("unit_sample", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
@@ -269,7 +270,7 @@ struct Ctx {
   DevBuf table;
   StepScalars* d_sc = nullptr;
   StepScalars* h_sc = nullptr;  // pinned
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t pool_bytes = 0, peak_pool_bytes = 0;
   size_t free_at_create = 0;
   uint64_t launches = 0;
@@ -290,8 +291,11 @@ struct Ctx {
                                                 // boundary (modes 1-2 only where exact: R = 2, N - k <= 20)
     double partition_fill = 0.83;               // starting value of Ctx::partition_fill
     double slice_margin = 5.0;                  // predictive slicing: slice peak / mean slice peak
+    uint32_t unit_target = 1000;                // class-grouped partitions: planned candidates per partition
+    uint32_t unit_sample = 8;                   // class-grouped partitions: 1 in unit_sample parents sampled
   } tune;
   DevBuf tail;                   // TailControl + overflow list
+  DevBuf plan;                   // class-grouped partitions: histogram, bucket table, scan partials
   uint64_t pool_gen = 0;         // bumped whenever a pool buffer is allocated or freed
   GraphRecorder* rec = nullptr;  // row steps of the running contraction (use_graph)
   GraphPlan* graph = nullptr;    // captured contraction (use_graph)
@@ -335,6 +339,7 @@ static void ctx_free(Ctx* ctx) {
   buf_release(*ctx, ctx->front[1]);
   buf_release(*ctx, ctx->table);
   buf_release(*ctx, ctx->tail);
+  buf_release(*ctx, ctx->plan);
   if (ctx->d_sc) cudaFree(ctx->d_sc);
   if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
   for (auto& e : ctx->ev)
@@ -470,6 +475,9 @@ enum class StepStatus { Ok, NeedSplit };
 // partition configuration and the sizes the step saw.
 struct GraphStepRec {
   PartitionCfg pc{};
+  bool unit = false;  // class-grouped partitions: the plan is rebuilt on the device before the scatter
+  UnitClassPlan ucp{};
+  UnitPlanArgs upa{};
   u64 n_in = 0, terms = 0, out = 0, need_cap = 0;
   size_t region_bytes = 0, table_bytes = 0;
   bool final_step = false;
@@ -544,6 +552,32 @@ static u64 count_terms(Ctx& ctx, const Plan& p, const DevFrontier& f, bool site,
   return ctx.h_sc->terms;
 }
 
+static double binom(unsigned n, unsigned k) {
+  if (k > n) return 0;
+  double v = 1;
+  for (unsigned i = 1; i <= k; ++i) v = v * (double)(n - k + i) / (double)i;
+  return v;
+}
+
+// Class plan of a row step with `terms` successors whose columns hold
+// `filled` queens: the window width t puts about target / 2 candidates in a
+// class, and the bucket count is about twice the class count.
+static UnitClassPlan unit_class_plan(unsigned n, unsigned filled, u64 terms, u32 target) {
+  UnitClassPlan c{};
+  c.n = n;
+  const double per_class = std::max(64.0, target / 2.0);
+  const double groups = std::max(1.0, binom(n, std::min(filled, n)));
+  const double want = (double)terms / (groups * per_class);
+  unsigned t = want > 1.0 ? (unsigned)std::lround(std::log(want) / std::log(4.0)) : 0u;
+  t = std::min(t, std::min(7u, n / 2));
+  c.t = t;
+  const double classes = std::max(1.0, (double)terms / per_class);
+  unsigned lg = (unsigned)std::ceil(std::log2(classes)) + 1;
+  lg = std::max(10u, std::min(24u, lg));
+  c.lg = lg;
+  return c;
+}
+
 // One merge step (a row in row grain, a site in site grain), in place.
 static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site, unsigned site_idx, bool final_step,
                              RunStats& rs, unsigned row, StepOut* so_out) {
@@ -565,15 +599,50 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   const double narrow_parts = (double)so.terms / (ctx.partition_fill * partition_capacity(0));
   const bool want_wide = ctx.tune.wide_merge == 1 ||
                          (ctx.tune.wide_merge == 2 && narrow_parts > (double)ctx.tune.wide_above_parts);
-  const u32 wide = (want_wide && wide_merge_supported(p.R)) ? 1u : 0u;
+  // Class-grouped partitions (16-byte candidates, narrow merge CTAs).
+  const bool unit = partition && ctx.tune.scatter_kind == 3 && unit_scatter_supported(p.R);
+  const u32 wide = (!unit && want_wide && wide_merge_supported(p.R)) ? 1u : 0u;
   const u32 pcap = partition_capacity(wide);
   double mean = ctx.partition_fill * pcap;
+  double unit_target = ctx.tune.unit_target;
   for (int attempt = 0;; ++attempt) {
     u32 parts = 0, cstride = 1;
     u64 slots = 0;
     size_t table_bytes, region_bytes = 0;
     PartitionCfg tl{};  // two-level scatter plan (tl.tl_nb = 0: one-level)
-    if (partition) {
+    UnitClassPlan ucp{};
+    UnitPlanArgs upa{};
+    UnitPlanDev upd{};
+    if (unit) {
+      // Plan on the device from a sampled histogram of this step's successors;
+      // the host reads back the unit count to size the regions.
+      ucp = unit_class_plan(p.n, row + 1, so.terms, (u32)unit_target);
+      upa.lg = ucp.lg;
+      upa.sample = ctx.tune.unit_sample;
+      upa.target = (u64)unit_target;
+      const size_t plan_bytes = unit_plan_scratch_bytes(upa.lg);
+      if (ctx.plan.bytes < plan_bytes) {
+        buf_release(ctx, ctx.plan);
+        if (ctx.pool_bytes + plan_bytes > p.budget) buf_release(ctx, ctx.table);
+        buf_reserve(ctx, ctx.plan, plan_bytes, p.budget, "partition plan");
+      }
+      cuda_check(cudaEventRecord(ctx.ev[3], ctx.stream), "event");
+      cuda_check(launch_unit_plan(view_of(p, ctx.front[0], f.cap), n_in, ucp, upa, ctx.plan.ptr, ctx.sms, ctx.stream,
+                                  &upd),
+                 "partition plan kernels");
+      cuda_check(cudaEventRecord(ctx.ev[4], ctx.stream), "event");
+      UnitPlanTotals tot{};
+      cuda_check(cudaMemcpyAsync(&tot, upd.totals, sizeof tot, cudaMemcpyDeviceToHost, ctx.stream), "plan totals");
+      cuda_check(cudaStreamSynchronize(ctx.stream), "plan synchronize");
+      ctx.d2h_bytes += sizeof tot;
+      rs.launches += 4;
+      if (tot.units == 0 || tot.units > 0xffffffffull)
+        fail(QPEPS_ERR_CAPACITY, row_msg("partition plan out of range at row", row + 1));
+      parts = (u32)tot.units;
+      region_bytes = (size_t)parts * pcap * candidate_bytes(p.R);
+      cstride = (parts <= ctx.tune.spread_cursors_below) ? 8u : 1u;
+      table_bytes = region_bytes + ((size_t)parts * 4 * cstride + 255) / 256 * 256;
+    } else if (partition) {
       const u64 parts64 = std::max<u64>(1, (u64)((double)so.terms / mean) + 1);
       if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
       parts = (u32)parts64;
@@ -622,7 +691,10 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     else
       cuda_check(cudaMemsetAsync(ctx.table.ptr, 0, table_bytes, ctx.stream), "clear hash table");
     cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
-    if (partition)
+    if (unit)
+      cuda_check(launch_unit_scatter(pc, view, n_in, ucp, upd.table, regions, cursors, ctx.d_sc, ctx.stream),
+                 "class scatter kernel");
+    else if (partition)
       cuda_check(launch_partition_scatter(pc, view, n_in, p.n, regions, cursors, ctx.d_sc, ctx.stream),
                  "partition scatter kernel");
     else if (site)
@@ -645,15 +717,22 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
       // The merge kernel saw the flag and wrote nothing: the input is intact.
       if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, row_msg("partition overflow persists at row", row + 1));
       mean *= 0.6;
+      unit_target = std::max(256.0, unit_target * 0.7);
       ctx.partition_fill = std::max(0.3, ctx.partition_fill * 0.8);  // keep a wider margin for this context
       (void)terms;
       continue;
     }
     if (ctx.h_sc->error & kErrProbeLimit) fail(QPEPS_ERR_CAPACITY, row_msg("hash probe bound exceeded at row", row + 1));
     if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, row_msg("device capacity error at row", row + 1));
-    float ms_a = 0, ms_b = 0;
+    float ms_a = 0, ms_b = 0, ms_plan = 0;
     cudaEventElapsedTime(&ms_a, ctx.ev[0], ctx.ev[1]);
     cudaEventElapsedTime(&ms_b, ctx.ev[1], ctx.ev[2]);
+    if (unit) {
+      // The plan kernels belong to the scatter's side of the step (as in a
+      // CUDA-graph replay, where they run back to back with it).
+      cudaEventElapsedTime(&ms_plan, ctx.ev[3], ctx.ev[4]);
+      ms_a += ms_plan;
+    }
     so.out = ctx.h_sc->out_count;
     so.exact_sum = ctx.h_sc->weight_sum[0];
     for (int r = 0; r < p.Rc; ++r) {
@@ -667,6 +746,9 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
       } else {
         GraphStepRec g;
         g.pc = pc;
+        g.unit = unit;
+        g.ucp = ucp;
+        g.upa = upa;
         g.n_in = n_in;
         g.terms = terms;
         g.out = so.out;
@@ -1398,6 +1480,7 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
     seed_bytes += c.count * eb;
     for (const GraphStepRec& st : c.steps) {
       if (st.terms && (st.need_cap > cap || st.table_bytes > ctx.table.bytes)) return;
+      if (st.terms && st.unit && (!ctx.plan.ptr || unit_plan_scratch_bytes(st.upa.lg) > ctx.plan.bytes)) return;
       ++nsteps;
     }
   }
@@ -1455,7 +1538,16 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
         void* regions = ctx.table.ptr;
         uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + st.region_bytes);
         ok(cudaMemsetAsync(cursors, 0, (size_t)st.pc.parts * 4 * st.pc.cursor_stride, ctx.stream));
-        ok(launch_partition_scatter(st.pc, view, st.n_in, p.n, regions, cursors, sc, ctx.stream));
+        if (st.unit) {
+          // The plan is a function of the boundary's keys only: the replay
+          // rebuilds the recorded one.
+          UnitPlanDev upd{};
+          ok(launch_unit_plan(view, st.n_in, st.ucp, st.upa, ctx.plan.ptr, ctx.sms, ctx.stream, &upd));
+          ok(launch_unit_scatter(st.pc, view, st.n_in, st.ucp, upd.table, regions, cursors, sc, ctx.stream));
+          g->launches += 4;
+        } else {
+          ok(launch_partition_scatter(st.pc, view, st.n_in, p.n, regions, cursors, sc, ctx.stream));
+        }
         ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
         ok(launch_partition_merge(st.pc, regions, cursors, view, p.n, !st.final_step, sc, ctx.stream));
         ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
@@ -2199,12 +2291,17 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
   q.fold_weights = t.fold_weights;
   q.partition_fill = t.partition_fill;
   q.slice_margin = t.slice_margin;
+  q.unit_target = t.unit_target;
+  q.unit_sample = t.unit_sample;
   return q;
 }
 
 static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.struct_size != sizeof(qpeps_tuning)) fail(QPEPS_ERR_INVALID, "qpeps_tuning.struct_size mismatch");
-  if (q.scatter_kind > 2) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0, 1 or 2");
+  if (q.scatter_kind > 3) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0, 1, 2 or 3");
+  if (q.unit_target < 256 || q.unit_target > 2048) fail(QPEPS_ERR_INVALID, "unit_target must be in [256, 2048]");
+  if (q.unit_sample < 1 || q.unit_sample > 64 || (q.unit_sample & (q.unit_sample - 1)))
+    fail(QPEPS_ERR_INVALID, "unit_sample must be a power of two in [1, 64]");
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
@@ -2222,6 +2319,8 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   t.fold_weights = q.fold_weights;
   t.partition_fill = q.partition_fill;
   t.slice_margin = q.slice_margin;
+  t.unit_target = q.unit_target;
+  t.unit_sample = q.unit_sample;
   return t;
 }
 

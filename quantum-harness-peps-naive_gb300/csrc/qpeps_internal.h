@@ -142,6 +142,42 @@ size_t two_level_extra_bytes(const PartitionCfg& pc);
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* scalars, cudaStream_t stream);
 
+// Class-grouped partitions (scatter_kind 3, 16-byte candidates). A
+// candidate's class is its columns and the t outermost diagonal pairs; classes
+// hash into 2^lg buckets (four sibling classes, equal but for pair 0, in
+// consecutive buckets), and a plan maps each bucket to a run of "units"
+// (merge partitions of `cap` slots) from a sampled histogram.
+struct UnitClassPlan {
+  unsigned n;   // board size
+  unsigned t;   // window pairs (0: columns only); t <= n / 2
+  unsigned lg;  // log2 of the bucket count (>= 3 when t >= 1)
+};
+struct UnitPlanArgs {
+  uint32_t lg;      // log2 of the bucket count
+  uint32_t sample;  // one parent block of 512 in `sample` is counted
+  uint64_t target;  // planned candidates per unit
+};
+struct UnitPlanTotals {
+  unsigned long long small_units;  // units of packed small buckets (unit ids [0, small_units))
+  unsigned long long units;        // all units (the merge's partition count)
+  unsigned long long small_e;      // estimated candidates of the packed buckets
+  unsigned long long pad;
+};
+struct UnitPlanDev {
+  const uint2* table = nullptr;         // per bucket {first unit, units}
+  UnitPlanTotals* totals = nullptr;     // device
+};
+bool unit_scatter_supported(int residues);
+// Device scratch of a plan with 2^lg buckets (histogram, table, scan partials, totals).
+size_t unit_plan_scratch_bytes(uint32_t lg);
+// Sampled histogram of the step's successors and the bucket -> units table;
+// the unit count lands in out->totals (device) for the host to read.
+cudaError_t launch_unit_plan(const FrontierView& in, uint64_t n_in, const UnitClassPlan& c, const UnitPlanArgs& a,
+                             void* scratch, int sms, cudaStream_t stream, UnitPlanDev* out);
+cudaError_t launch_unit_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in,
+                                const UnitClassPlan& c, const uint2* table, void* regions, uint32_t* cursors,
+                                StepScalars* scalars, cudaStream_t stream);
+
 cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                    const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
                                    cudaStream_t stream);

@@ -34,7 +34,7 @@ def tctx(qp):
 
 
 @pytest.mark.parametrize("scatter,ppl,merge,wide,fold", [
-    combo for combo in itertools.product((0, 1, 2), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
+    combo for combo in itertools.product((0, 1, 2, 3), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
 ])
 def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold):
     tctx.set_tuning(scatter_kind=scatter, parents_per_lane=ppl, merge_kind=merge, wide_merge=wide,
@@ -45,6 +45,51 @@ def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wi
         assert got.count == want["count"]
         assert got.peak_states == want["peak_states"]
         assert [l.output_states for l in got.layers] == [l["output_states"] for l in want["layers"]]
+
+
+@pytest.mark.parametrize("n", [14, 16, 17])
+def test_class_scatter_equals_the_window_scatter(tctx, qp, n):
+    # Class-grouped partitions: other partitions, the same merged boundary,
+    # so the same counts and per-row metrics, eagerly and under graph replay.
+    ref = tctx.contract_rows(n)
+    tctx.set_tuning(scatter_kind=qp.SCATTER_CLASS)
+    got = tctx.contract_rows(n)
+    assert got.count == ref.count == qp.known_count(n)
+    assert _layers(got) == _layers(ref)
+    assert got.peak_states == ref.peak_states
+    first = tctx.contract_rows(n, use_graph=1)
+    again = tctx.contract_rows(n, use_graph=1)
+    assert again.device["gpu_launches"] < first.device["gpu_launches"]  # replayed
+    assert first.count == again.count == ref.count
+    assert _layers(again) == _layers(ref)
+
+
+def test_class_scatter_undersized_plan_retries_exactly(tctx, qp, oracle):
+    # A coarse sample (1 parent in 64) with small planned partitions makes the
+    # plan's estimates noisy; a partition that overflows makes the merge write
+    # nothing and the row runs again with more partitions.
+    tctx.set_tuning(scatter_kind=qp.SCATTER_CLASS, unit_sample=64, unit_target=1800)
+    for n in (12, 15):
+        got = tctx.contract_rows(n)
+        assert got.count == qp.known_count(n)
+        if n <= 12:
+            want = _oracle(oracle, n)
+            assert [l.output_states for l in got.layers] == [l["output_states"] for l in want["layers"]]
+
+
+@pytest.mark.parametrize("R", [1, 2])
+def test_class_scatter_residue_planes_prefixes_and_budget(tctx, qp, oracle, R):
+    tctx.set_tuning(scatter_kind=qp.SCATTER_CLASS, fold_weights=0)
+    n = 12
+    got = tctx.contract_rows(n, residues=R)
+    want = _oracle(oracle, n)
+    assert got.count == want["count"]
+    assert [(l.output_states, l.output_weight) for l in got.layers] == [
+        (l["output_states"], l["output_weight"]) for l in want["layers"]]
+    for prefix in ([3], [1, 4], [0, 2, 5]):
+        assert tctx.count(13, prefix) == oracle.contract(13, symmetry=False, prefix=prefix)["count"]
+    small = tctx.contract_rows(14, device_budget_bytes=16 << 20)
+    assert small.count == qp.known_count(14) and small.device["batches"] > 1
 
 
 @pytest.mark.parametrize("n", [15, 16, 17])
@@ -90,7 +135,7 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 
 @pytest.mark.parametrize("field,value", [
-    ("scatter_kind", 3), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
+    ("scatter_kind", 4), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
     ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 3),
 ])
 def test_out_of_range_tuning_is_rejected_and_kept(tctx, qp, field, value):
