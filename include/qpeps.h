@@ -241,6 +241,10 @@ typedef struct qpeps_tuning {
   uint32_t unit_target;          /* QPEPS_SCATTER_CLASS: planned candidates per partition, 256..2048 */
   uint32_t unit_sample;          /* QPEPS_SCATTER_CLASS: 1 in unit_sample parents sampled for the plan
                                     (a power of two, 1..64) */
+  uint32_t batch_lanes;          /* CUDA-graph replay: independent device batches run concurrently on
+                                    this many streams, each with its own buffers (1..8; lanes beyond
+                                    the first only while the device budget holds their buffers) */
+  uint32_t reserved;
 } qpeps_tuning;
 
 /* Library defaults (what a new context starts with). */

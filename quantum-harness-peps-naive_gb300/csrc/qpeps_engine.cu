@@ -293,6 +293,7 @@ struct Ctx {
     double slice_margin = 5.0;                  // predictive slicing: slice peak / mean slice peak
     uint32_t unit_target = 1000;                // class-grouped partitions: planned candidates per partition
     uint32_t unit_sample = 8;                   // class-grouped partitions: 1 in unit_sample parents sampled
+    uint32_t batch_lanes = 2;                   // CUDA-graph replay: device batches run on this many streams
   } tune;
   DevBuf tail;                   // TailControl + overflow list
   DevBuf plan;                   // class-grouped partitions: histogram, bucket table, scan partials
@@ -1416,6 +1417,21 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
 // against the recorded run before it answers; on any difference it drops the
 // graph and contracts eagerly.
 
+// Device batches are independent sub-contractions (their results add), so
+// the graph runs them on `batch_lanes` streams at once: each lane has its own
+// boundary, partition regions and plan scratch (lane 0 borrows the context's)
+// and takes whole batches, balanced by their recorded successor counts; the
+// kernels of different lanes overlap on the device. The start event, the
+// lanes' fork and join and the read-back of all scalars stay on the context's
+// stream.
+struct GraphLane {
+  cudaStream_t stream = nullptr;  // lane 0: the context's stream
+  DevBuf front, table, plan;      // owned by lanes >= 1
+  u64 cap = 0;                    // boundary capacity (entries)
+  cudaEvent_t join = nullptr;
+  std::vector<size_t> chunks;     // indices into GraphPlan::chunks, in launch order
+};
+
 struct GraphPlan {
   unsigned n = 0;
   std::vector<uint32_t> prefix;
@@ -1424,14 +1440,19 @@ struct GraphPlan {
   uint64_t pool_gen = 0;
   Contraction base;
   std::vector<GraphChunkRec> chunks;
+  std::vector<size_t> step_base;  // first scalars slot of each chunk
   cudaGraphExec_t exec = nullptr;
   void* h_seeds = nullptr;  // pinned: every batch's seed keys and residue planes, packed
+  std::vector<size_t> seed_off;
   size_t seed_bytes = 0;
   StepScalars* d_scal = nullptr;
   StepScalars* h_scal = nullptr;
   size_t nsteps = 0;
   uint64_t launches = 0;
-  std::vector<cudaEvent_t> ev;  // ev[0] start, then one after every kernel
+  size_t lane_bytes = 0;          // device memory held by lanes >= 1
+  std::vector<GraphLane> lanes;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> ev;    // three per step with work: start, after the scatter, after the merge
 };
 
 static void graph_free(Ctx& ctx) {
@@ -1443,6 +1464,15 @@ static void graph_free(Ctx& ctx) {
   if (g->h_scal) cudaFreeHost(g->h_scal);
   for (cudaEvent_t e : g->ev)
     if (e) cudaEventDestroy(e);
+  if (g->fork) cudaEventDestroy(g->fork);
+  for (size_t l = 0; l < g->lanes.size(); ++l) {
+    GraphLane& L = g->lanes[l];
+    if (L.join) cudaEventDestroy(L.join);
+    if (l == 0) continue;
+    for (DevBuf* b : {&L.front, &L.table, &L.plan})
+      if (b->ptr) cudaFree(b->ptr);
+    if (L.stream) cudaStreamDestroy(L.stream);
+  }
   delete g;
   ctx.graph = nullptr;
 }
@@ -1473,17 +1503,59 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
       p.key_bits != 64 || !ctx.front[0].ptr || !ctx.table.ptr)
     return;
   const size_t eb = entry_bytes(p), kb = key_bytes(p);
-  const u64 cap = ctx.front[0].bytes / eb;
+  const u64 cap0 = ctx.front[0].bytes / eb;
   size_t seed_bytes = 0, nsteps = 0;
-  for (const GraphChunkRec& c : rec.chunks) {
-    if (c.count > cap) return;
+  // Per chunk: boundary capacity, region and plan bytes it needs, and its work.
+  const size_t nc = rec.chunks.size();
+  std::vector<u64> need_cap(nc, 0), work(nc, 0);
+  std::vector<size_t> need_table(nc, 0), need_plan(nc, 0);
+  for (size_t i = 0; i < nc; ++i) {
+    const GraphChunkRec& c = rec.chunks[i];
+    need_cap[i] = std::max<u64>(c.count, 1);
     seed_bytes += c.count * eb;
     for (const GraphStepRec& st : c.steps) {
-      if (st.terms && (st.need_cap > cap || st.table_bytes > ctx.table.bytes)) return;
-      if (st.terms && st.unit && (!ctx.plan.ptr || unit_plan_scratch_bytes(st.upa.lg) > ctx.plan.bytes)) return;
       ++nsteps;
+      if (!st.terms) continue;
+      need_cap[i] = std::max(need_cap[i], st.need_cap);
+      need_table[i] = std::max(need_table[i], st.table_bytes);
+      if (st.unit) need_plan[i] = std::max(need_plan[i], unit_plan_scratch_bytes(st.upa.lg));
+      work[i] += st.terms;
     }
+    if (need_cap[i] > cap0 || need_table[i] > ctx.table.bytes || (need_plan[i] && need_plan[i] > ctx.plan.bytes))
+      return;  // lane 0 runs in the context's buffers
   }
+  // Lanes: whole batches, heaviest first to the least loaded lane; a lane
+  // beyond the first is kept only while the device budget holds its buffers.
+  unsigned nl = (unsigned)std::max<u64>(1, std::min<u64>(ctx.tune.batch_lanes, nc));
+  std::vector<size_t> order(nc);
+  for (size_t i = 0; i < nc; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return work[a] > work[b]; });
+  std::vector<std::vector<size_t>> assign;
+  std::vector<size_t> lane_bytes;
+  for (;; --nl) {
+    assign.assign(nl, {});
+    std::vector<u64> load(nl, 0);
+    for (size_t i : order) {
+      const size_t l = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+      assign[l].push_back(i);
+      load[l] += work[i] + 1;
+    }
+    lane_bytes.assign(nl, 0);
+    size_t extra = 0;
+    for (unsigned l = 1; l < nl; ++l) {
+      u64 cap = 1;
+      size_t tb = 0, pb = 0;
+      for (size_t i : assign[l]) {
+        cap = std::max(cap, need_cap[i]);
+        tb = std::max(tb, need_table[i]);
+        pb = std::max(pb, need_plan[i]);
+      }
+      lane_bytes[l] = cap * eb + tb + pb;
+      extra += lane_bytes[l];
+    }
+    if (nl == 1 || ctx.pool_bytes + extra <= p.budget) break;
+  }
+  for (auto& a : assign) std::sort(a.begin(), a.end());  // recorded order within a lane
   GraphPlan* g = new GraphPlan();
   ctx.graph = g;
   g->n = n;
@@ -1499,59 +1571,119 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
     if (e != cudaSuccess) throw Failure{QPEPS_ERR_CUDA, cudaGetErrorString(e)};
   };
   try {
+    g->lanes.resize(nl);
+    for (unsigned l = 0; l < nl; ++l) {
+      GraphLane& L = g->lanes[l];
+      L.chunks = assign[l];
+      ok(cudaEventCreateWithFlags(&L.join, cudaEventDisableTiming));
+      if (l == 0) {
+        L.stream = ctx.stream;
+        L.front = ctx.front[0];
+        L.table = ctx.table;
+        L.plan = ctx.plan;
+        L.cap = cap0;
+        continue;
+      }
+      ok(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+      u64 cap = 1;
+      size_t tb = 0, pb = 0;
+      for (size_t i : L.chunks) {
+        cap = std::max(cap, need_cap[i]);
+        tb = std::max(tb, need_table[i]);
+        pb = std::max(pb, need_plan[i]);
+      }
+      L.cap = cap;
+      ok(cudaMalloc(&L.front.ptr, cap * eb));
+      L.front.bytes = cap * eb;
+      ok(cudaMalloc(&L.table.ptr, std::max<size_t>(tb, 256)));
+      L.table.bytes = std::max<size_t>(tb, 256);
+      if (pb) {
+        ok(cudaMalloc(&L.plan.ptr, pb));
+        L.plan.bytes = pb;
+      }
+      g->lane_bytes += L.front.bytes + L.table.bytes + L.plan.bytes;
+    }
+    ok(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming));
     ok(cudaMallocHost(&g->h_seeds, std::max<size_t>(seed_bytes, 16)));
     g->seed_bytes = seed_bytes;
     ok(cudaMalloc(&g->d_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars)));
     ok(cudaMallocHost(&g->h_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars)));
     // Seeds: each batch's keys then its residue planes, packed in pinned
     // memory; every replay uploads them again (the graph's copy nodes).
-    size_t off = 0;
-    for (const GraphChunkRec& c : g->chunks) {
+    size_t off = 0, si = 0, nev = 0;
+    g->seed_off.resize(g->chunks.size());
+    g->step_base.resize(g->chunks.size());
+    for (size_t i = 0; i < g->chunks.size(); ++i) {
+      const GraphChunkRec& c = g->chunks[i];
+      g->seed_off[i] = off;
+      g->step_base[i] = si;
       std::memcpy(static_cast<char*>(g->h_seeds) + off, c.keys.data(), c.count * kb);
       std::memcpy(static_cast<char*>(g->h_seeds) + off + c.count * kb, c.res.data(), c.count * 4u * p.R);
       off += c.count * eb;
+      si += c.steps.size();
+      for (const GraphStepRec& st : c.steps) nev += st.terms ? 3 : 0;
     }
-    size_t nev = 1;
-    for (const GraphChunkRec& c : g->chunks)
-      for (const GraphStepRec& st : c.steps) nev += st.terms ? 2 : 0;
     g->ev.assign(nev, nullptr);
     for (cudaEvent_t& e : g->ev) ok(cudaEventCreate(&e));
+    // Events of step j of chunk i: 3 * (rank of the step among steps with work).
+    std::vector<size_t> ev_base(g->chunks.size());
+    size_t ecount = 0;
+    for (size_t i = 0; i < g->chunks.size(); ++i) {
+      ev_base[i] = ecount;
+      for (const GraphStepRec& st : g->chunks[i].steps) ecount += st.terms ? 3 : 0;
+    }
 
     ok(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeRelaxed));
     capturing = true;
     ok(cudaMemsetAsync(g->d_scal, 0, std::max<size_t>(nsteps, 1) * sizeof(StepScalars), ctx.stream));
-    size_t ei = 0, si = 0;
-    ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
-    char* front = static_cast<char*>(ctx.front[0].ptr);
-    FrontierView view = view_of(p, ctx.front[0], cap);
-    off = 0;
-    for (const GraphChunkRec& c : g->chunks) {
-      const char* sd = static_cast<const char*>(g->h_seeds) + off;
-      ok(cudaMemcpyAsync(front, sd, c.count * kb, cudaMemcpyHostToDevice, ctx.stream));
-      for (int r = 0; r < p.R; ++r)
-        ok(cudaMemcpyAsync(front + cap * kb + (size_t)r * cap * 4, sd + c.count * kb + (size_t)r * c.count * 4,
-                           c.count * 4, cudaMemcpyHostToDevice, ctx.stream));
-      off += c.count * eb;
-      for (const GraphStepRec& st : c.steps) {
-        StepScalars* sc = g->d_scal + si++;
-        if (!st.terms) continue;
-        void* regions = ctx.table.ptr;
-        uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx.table.ptr) + st.region_bytes);
-        ok(cudaMemsetAsync(cursors, 0, (size_t)st.pc.parts * 4 * st.pc.cursor_stride, ctx.stream));
-        if (st.unit) {
-          // The plan is a function of the boundary's keys only: the replay
-          // rebuilds the recorded one.
-          UnitPlanDev upd{};
-          ok(launch_unit_plan(view, st.n_in, st.ucp, st.upa, ctx.plan.ptr, ctx.sms, ctx.stream, &upd));
-          ok(launch_unit_scatter(st.pc, view, st.n_in, st.ucp, upd.table, regions, cursors, sc, ctx.stream));
-          g->launches += 4;
-        } else {
-          ok(launch_partition_scatter(st.pc, view, st.n_in, p.n, regions, cursors, sc, ctx.stream));
+    ok(cudaEventRecord(g->fork, ctx.stream));
+    for (unsigned l = 1; l < nl; ++l) ok(cudaStreamWaitEvent(g->lanes[l].stream, g->fork, 0));
+    for (GraphLane& L : g->lanes) {
+      cudaStream_t st_ = L.stream;
+      char* front = static_cast<char*>(L.front.ptr);
+      DevBuf lane_front = L.front;
+      const FrontierView view = view_of(p, lane_front, L.cap);
+      for (size_t i : L.chunks) {
+        const GraphChunkRec& c = g->chunks[i];
+        const char* sd = static_cast<const char*>(g->h_seeds) + g->seed_off[i];
+        size_t ei = ev_base[i];
+        size_t sj = g->step_base[i];
+        bool first = true;
+        for (const GraphStepRec& st : c.steps) {
+          StepScalars* sc = g->d_scal + sj++;
+          if (!st.terms) continue;
+          ok(cudaEventRecordWithFlags(g->ev[ei], st_, cudaEventRecordExternal));
+          if (first) {
+            ok(cudaMemcpyAsync(front, sd, c.count * kb, cudaMemcpyHostToDevice, st_));
+            for (int r = 0; r < p.R; ++r)
+              ok(cudaMemcpyAsync(front + L.cap * kb + (size_t)r * L.cap * 4,
+                                 sd + c.count * kb + (size_t)r * c.count * 4, c.count * 4, cudaMemcpyHostToDevice,
+                                 st_));
+            first = false;
+          }
+          void* regions = L.table.ptr;
+          uint32_t* cursors = reinterpret_cast<uint32_t*>(static_cast<char*>(L.table.ptr) + st.region_bytes);
+          ok(cudaMemsetAsync(cursors, 0, (size_t)st.pc.parts * 4 * st.pc.cursor_stride, st_));
+          if (st.unit) {
+            // The plan is a function of the boundary's keys only: the replay
+            // rebuilds the recorded one.
+            UnitPlanDev upd{};
+            ok(launch_unit_plan(view, st.n_in, st.ucp, st.upa, L.plan.ptr, ctx.sms, st_, &upd));
+            ok(launch_unit_scatter(st.pc, view, st.n_in, st.ucp, upd.table, regions, cursors, sc, st_));
+            g->launches += 4;
+          } else {
+            ok(launch_partition_scatter(st.pc, view, st.n_in, p.n, regions, cursors, sc, st_));
+          }
+          ok(cudaEventRecordWithFlags(g->ev[ei + 1], st_, cudaEventRecordExternal));
+          ok(launch_partition_merge(st.pc, regions, cursors, view, p.n, !st.final_step, sc, st_));
+          ok(cudaEventRecordWithFlags(g->ev[ei + 2], st_, cudaEventRecordExternal));
+          ei += 3;
+          g->launches += 2;
         }
-        ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
-        ok(launch_partition_merge(st.pc, regions, cursors, view, p.n, !st.final_step, sc, ctx.stream));
-        ok(cudaEventRecordWithFlags(g->ev[ei++], ctx.stream, cudaEventRecordExternal));
-        g->launches += 2;
+      }
+      if (st_ != ctx.stream) {
+        ok(cudaEventRecord(L.join, st_));
+        ok(cudaStreamWaitEvent(ctx.stream, L.join, 0));
       }
     }
     ok(cudaMemcpyAsync(g->h_scal, g->d_scal, std::max<size_t>(nsteps, 1) * sizeof(StepScalars),
@@ -1562,6 +1694,7 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
     cudaGraphDestroy(graph);
     graph = nullptr;
     g->pool_gen = ctx.pool_gen;
+    ctx.peak_pool_bytes = std::max(ctx.peak_pool_bytes, ctx.pool_bytes + g->lane_bytes);
   } catch (const Failure&) {
     if (capturing) {
       cudaGraph_t dead = nullptr;
@@ -1606,18 +1739,16 @@ static bool graph_replay(Ctx& ctx, unsigned n, const qpeps_options& o, const uin
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
   out.rs.device_ms = ms;
+  // Kernel times per step (with several lanes they overlap in time, so their
+  // sum can exceed device_ms).
   out.rs.scatter_ms = out.rs.merge_ms = 0;
-  size_t ei = 1;
-  for (const GraphChunkRec& c : g->chunks)
-    for (const GraphStepRec& st : c.steps) {
-      if (!st.terms) continue;
-      float a = 0, b = 0;
-      cudaEventElapsedTime(&a, g->ev[ei - 1], g->ev[ei]);
-      cudaEventElapsedTime(&b, g->ev[ei], g->ev[ei + 1]);
-      out.rs.scatter_ms += a;
-      out.rs.merge_ms += b;
-      ei += 2;
-    }
+  for (size_t ei = 0; ei + 2 < g->ev.size(); ei += 3) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, g->ev[ei], g->ev[ei + 1]);
+    cudaEventElapsedTime(&b, g->ev[ei + 1], g->ev[ei + 2]);
+    out.rs.scatter_ms += a;
+    out.rs.merge_ms += b;
+  }
   out.rs.launches = g->launches;
   out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return true;
@@ -2293,6 +2424,7 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
   q.slice_margin = t.slice_margin;
   q.unit_target = t.unit_target;
   q.unit_sample = t.unit_sample;
+  q.batch_lanes = t.batch_lanes;
   return q;
 }
 
@@ -2302,6 +2434,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.unit_target < 256 || q.unit_target > 2048) fail(QPEPS_ERR_INVALID, "unit_target must be in [256, 2048]");
   if (q.unit_sample < 1 || q.unit_sample > 64 || (q.unit_sample & (q.unit_sample - 1)))
     fail(QPEPS_ERR_INVALID, "unit_sample must be a power of two in [1, 64]");
+  if (q.batch_lanes < 1 || q.batch_lanes > 8) fail(QPEPS_ERR_INVALID, "batch_lanes must be in [1, 8]");
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
@@ -2321,6 +2454,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   t.slice_margin = q.slice_margin;
   t.unit_target = q.unit_target;
   t.unit_sample = q.unit_sample;
+  t.batch_lanes = q.batch_lanes;
   return t;
 }
 

@@ -67,3 +67,29 @@ def test_eager_run_between_replays_keeps_results_exact(gctx, qp):
     gctx.contract_rows(15)                               # grows the context's buffers
     r = gctx.contract_rows(14, use_graph=1)
     assert r.count == qp.known_count(14)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 3])
+def test_concurrent_batch_lanes_replay_exactly(gctx, qp, lanes):
+    # Device batches are independent sub-contractions: the replay runs them on
+    # `batch_lanes` streams with a buffer set each; every row's metrics and
+    # the count equal the eager run's, whichever lane ran which batch.
+    gctx.set_tuning(batch_lanes=lanes)
+    budget = 48 << 20  # several device batches
+    eager = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
+    assert eager.device["batches"] > 1
+    replay = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
+    again = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
+    assert replay.device["gpu_launches"] < eager.device["gpu_launches"]  # replayed
+    assert eager.count == replay.count == again.count == qp.known_count(15)
+    assert _metrics(replay) == _metrics(eager) == _metrics(again)
+
+
+def test_lanes_with_class_partitions_replay_exactly(gctx, qp):
+    gctx.set_tuning(batch_lanes=2, scatter_kind=qp.SCATTER_CLASS)
+    budget = 48 << 20
+    eager = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
+    replay = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
+    assert replay.device["gpu_launches"] < eager.device["gpu_launches"]
+    assert eager.count == replay.count == qp.known_count(15)
+    assert _metrics(replay) == _metrics(eager)
