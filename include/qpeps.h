@@ -219,6 +219,8 @@ int qpeps_explicit_frontier(void* ctx, uint32_t n, uint32_t order, uint64_t supp
                                   and outermost diagonal signals, so a CTA's successors go to few
                                   partitions and are written as runs (16-byte candidates; the window
                                   scatter elsewhere) */
+#define QPEPS_SCATTER_DIRECT 4 /* each lane stores its own parents' successors: no shared-memory window,
+                                  no shuffles */
 #define QPEPS_MERGEK_SCAN 0    /* ballot/scan compaction over the whole table */
 #define QPEPS_MERGEK_CLAIM 1   /* claim list + first-claimant stores (default) */
 

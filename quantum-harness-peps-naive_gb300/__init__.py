@@ -44,6 +44,7 @@ SCATTER_SEARCH = 0
 SCATTER_WINDOW = 1
 SCATTER_TWO_LEVEL = 2
 SCATTER_CLASS = 3
+SCATTER_DIRECT = 4
 MERGEK_SCAN = 0
 MERGEK_CLAIM = 1
 

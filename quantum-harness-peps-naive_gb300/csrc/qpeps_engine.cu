@@ -2430,7 +2430,7 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
 
 static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.struct_size != sizeof(qpeps_tuning)) fail(QPEPS_ERR_INVALID, "qpeps_tuning.struct_size mismatch");
-  if (q.scatter_kind > 3) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0, 1, 2 or 3");
+  if (q.scatter_kind > 4) fail(QPEPS_ERR_INVALID, "scatter_kind must be 0..4");
   if (q.unit_target < 256 || q.unit_target > 2048) fail(QPEPS_ERR_INVALID, "unit_target must be in [256, 2048]");
   if (q.unit_sample < 1 || q.unit_sample > 64 || (q.unit_sample & (q.unit_sample - 1)))
     fail(QPEPS_ERR_INVALID, "unit_sample must be a power of two in [1, 64]");

@@ -348,6 +348,119 @@ __global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_
   if (overflow) atomicOr(&sc->error, kErrOverflow);
 }
 
+// Direct variant of the scatter (scatter_kind 4). Each lane expands its own
+// kPPL parents and issues their successors' cursor atomics and candidate
+// stores itself, kDB successors per round, with no shared-memory window and
+// no shuffles: per candidate the load/store pipe carries one atomic and one
+// store, where the window scatter adds a shared-memory write and read. Lanes
+// with fewer successors idle in the rounds the warp's busiest lane still
+// needs. Same inputs, outputs and overflow rule as the other scatters.
+constexpr int kDB = 4;  // successors per lane per round (atomics in flight per lane)
+
+template <int R, int BLOCK, int kPPL, typename Layout>
+__global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_direct_kernel(const u64* __restrict__ keys,
+                                                                          const u32* __restrict__ res, u64 res_stride,
+                                                                          u64 n_in, Layout L,
+                                                                          Cand<R>* __restrict__ regions,
+                                                                          u32* __restrict__ cursors, u32 cstride,
+                                                                          u32 parts, u32 cap,
+                                                                          StepScalars* __restrict__ sc) {
+  constexpr int WARPS = BLOCK / 32;
+  constexpr int PW = 32 * kPPL;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const u64 gwarp = (u64)blockIdx.x * WARPS + wid;
+  const u64 stride = (u64)gridDim.x * WARPS * PW;
+  bool overflow = false;
+  const u64 policy = l2_keep_policy();
+  u64 nkey[kPPL];
+  u32 nw[kPPL][R];
+  auto fetch = [&](u64 base) {
+#pragma unroll
+    for (int q = 0; q < kPPL; ++q) {
+      const u64 i = base + q * 32 + lane;
+      nkey[q] = kEmptyKey;
+      if (i < n_in) {
+        nkey[q] = __ldcs(keys + i);
+#pragma unroll
+        for (int r = 0; r < R; ++r) nw[q][r] = __ldcs(res + r * res_stride + i);
+      }
+    }
+  };
+  u64 base = gwarp * PW;
+  if (base < n_in) fetch(base);
+  for (; base < n_in; base += stride) {
+    u64 ckey[kPPL], fr[kPPL];
+    u32 cw[kPPL][R];
+#pragma unroll
+    for (int q = 0; q < kPPL; ++q) {
+      ckey[q] = nkey[q];
+      fr[q] = 0;
+      if (ckey[q] != kEmptyKey) {
+        const State s = L.unpack(ckey[q]);
+        fr[q] = ~(s.cols | s.dr | s.dl) & L.mask_of(ckey[q]);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) cw[q][r] = nw[q][r];
+    }
+    if (base + stride < n_in) fetch(base + stride);
+    int q = 0;  // this lane's current parent
+    while (q < kPPL && !fr[q]) ++q;
+    while (__any_sync(kFullMask, q < kPPL)) {
+      Cand<R> c[kDB];
+      u32 part[kDB], pos[kDB];
+#pragma unroll
+      for (int k = 0; k < kDB; ++k) {
+        part[k] = 0xffffffffu;
+        if (q < kPPL) {
+          // q < kPPL implies fr[q] != 0; the parent index is dynamic, so pick
+          // its words with a small unrolled select.
+          u64 pk = ckey[0], pf = fr[0];
+          u32 pw[R];
+#pragma unroll
+          for (int r = 0; r < R; ++r) pw[r] = cw[0][r];
+#pragma unroll
+          for (int qq = 1; qq < kPPL; ++qq)
+            if (q == qq) {
+              pk = ckey[qq];
+              pf = fr[qq];
+#pragma unroll
+              for (int r = 0; r < R; ++r) pw[r] = cw[qq][r];
+            }
+          const u64 b = pf & (0ull - pf);
+          const State s = L.unpack(pk);
+          c[k].key = L.successor(pk, s, b);
+#pragma unroll
+          for (int r = 0; r < R; ++r) c[k].res[r] = pw[r];
+          part[k] = partition_of(fib_hash_a(c[k].key), parts);
+#pragma unroll
+          for (int qq = 0; qq < kPPL; ++qq)
+            if (q == qq) fr[qq] ^= b;
+          while (q < kPPL) {
+            u64 left = fr[0];
+#pragma unroll
+            for (int qq = 1; qq < kPPL; ++qq)
+              if (q == qq) left = fr[qq];
+            if (left) break;
+            ++q;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kDB; ++k)
+        if (part[k] != 0xffffffffu) pos[k] = atomicAdd(&cursors[(u64)part[k] * cstride], 1u);
+#pragma unroll
+      for (int k = 0; k < kDB; ++k)
+        if (part[k] != 0xffffffffu) {
+          if (pos[k] < cap)
+            store_cand_keep<R>(regions + (u64)part[k] * cap + pos[k], c[k], policy);
+          else
+            overflow = true;
+        }
+    }
+  }
+  if (overflow) atomicOr(&sc->error, kErrOverflow);
+}
+
 // ---------------------------------------------------------------------------
 // Merge. One CTA per partition at a time (persistent over partitions). All
 // candidate loads of a partition are issued together into registers; the
@@ -1118,7 +1231,13 @@ cudaError_t scatter_ppl(const PartitionCfg& pc, const FrontierView& in, u64 n_in
   u64 want = (n_in + kScatterBlock * PPL - 1) / (kScatterBlock * PPL);
   const u64 capb = (u64)pc.sms * 8;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
-  if (pc.scatter_kind != 0) {  // 2 without a two-level plan: the window scatter
+  if (pc.scatter_kind == 4) {
+    partition_scatter_direct_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
+        reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
+        pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
+    return cudaGetLastError();
+  }
+  if (pc.scatter_kind != 0) {  // 2 without a two-level plan, or 3 where it does not apply: the window scatter
     partition_scatter_list_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
         reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
         pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
