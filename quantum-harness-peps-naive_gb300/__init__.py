@@ -199,11 +199,11 @@ class Tuning(ctypes.Structure):
         ("unit_target", ctypes.c_uint32),
         ("unit_sample", ctypes.c_uint32),
         ("batch_lanes", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("merge_compact", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f not in ("struct_size", "reserved")}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "struct_size"}
 
 
 # Every symbol include/qpeps.h declares, with its ctypes signature.

@@ -294,6 +294,7 @@ struct Ctx {
     uint32_t unit_target = 1000;                // class-grouped partitions: planned candidates per partition
     uint32_t unit_sample = 8;                   // class-grouped partitions: 1 in unit_sample parents sampled
     uint32_t batch_lanes = 2;                   // CUDA-graph replay: device batches run on this many streams
+    uint32_t merge_compact = 1;                 // claim-list merge: 1 = first claimants write from registers
   } tune;
   DevBuf tail;                   // TailControl + overflow list
   DevBuf plan;                   // class-grouped partitions: histogram, bucket table, scan partials
@@ -682,6 +683,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
     PartitionCfg pc{p.R, ctx.sms, parts, pcap, p.R == 1 ? 3 : p.R == 2 ? 2 : 1, cstride, ctx.tune.parents_per_lane,
                     wide, ctx.tune.scatter_kind, ctx.tune.merge_kind,
                     p.w64 ? 2u : (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
+    pc.merge_regs = ctx.tune.merge_compact;
     pc.tl_nb = tl.tl_nb;
     pc.tl_p2 = tl.tl_p2;
     pc.tl_bcap = tl.tl_bcap;
@@ -2425,6 +2427,7 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
   q.unit_target = t.unit_target;
   q.unit_sample = t.unit_sample;
   q.batch_lanes = t.batch_lanes;
+  q.merge_compact = t.merge_compact;
   return q;
 }
 
@@ -2435,6 +2438,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.unit_sample < 1 || q.unit_sample > 64 || (q.unit_sample & (q.unit_sample - 1)))
     fail(QPEPS_ERR_INVALID, "unit_sample must be a power of two in [1, 64]");
   if (q.batch_lanes < 1 || q.batch_lanes > 8) fail(QPEPS_ERR_INVALID, "batch_lanes must be in [1, 8]");
+  if (q.merge_compact > 1) fail(QPEPS_ERR_INVALID, "merge_compact must be 0 or 1");
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
@@ -2455,6 +2459,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   t.unit_target = q.unit_target;
   t.unit_sample = q.unit_sample;
   t.batch_lanes = q.batch_lanes;
+  t.merge_compact = q.merge_compact;
   return t;
 }
 

@@ -672,7 +672,11 @@ __device__ __forceinline__ u64 one_plane(u32 w0, u32 w1) {
     return crt_fold2(w0, w1);
 }
 
-template <int R, int BLOCK, int H, int CAP, typename Layout, int kAcc = 0>
+// kRegs (fixed layout only): a key's first claimant keeps the key and its list
+// index in registers and writes the output entry itself after the last
+// barrier, reading only the accumulator from shared memory; the slot list is
+// never stored or read.
+template <int R, int BLOCK, int H, int CAP, typename Layout, int kAcc = 0, bool kRegs = false>
 __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<R>* __restrict__ regions,
                                                                      const u32* __restrict__ cursors, u32 cstride,
                                                                      u32 parts, u64* __restrict__ keys_out,
@@ -686,6 +690,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   constexpr bool kFold = kAcc != 0;  // one 64-bit accumulator plane
   static_assert(!kFold || R == 2, "the one-plane accumulators hold a residue pair or a weight's two words");
   static_assert(kAcc != 2 || !Layout::kSlotted, "exact weights are not used by the serving layout");
+  static_assert(!kRegs || !Layout::kSlotted, "register compaction is for the fixed layout");
   constexpr int AP = kFold ? 1 : R;  // accumulator planes
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* s_key = reinterpret_cast<u64*>(smem_raw);
@@ -724,6 +729,8 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     const u32 next = part + gridDim.x;
     const u32 next_cnt = next < parts ? cursors[(u64)next * cstride] : 0u;
     u32 slots[LPT];
+    u32 fidx[kRegs ? LPT : 1];   // list index of a first claimant (kRegs)
+    u64 fkey[kRegs ? LPT : 1];   // and its key, kept past the next partition's loads
     u32 fresh_bits = 0, dup_bits = 0;
 #pragma unroll
     for (int l = 0; l < LPT; ++l) {
@@ -762,7 +769,12 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
         u32 at = 0;
         if (lane == leader) at = atomicAdd(&s_nused, (u32)__popc(b));
         at = __shfl_sync(kFullMask, at, leader);
-        if (fresh) s_list[at + __popc(b & ((1u << lane) - 1u))] = slot;
+        if constexpr (kRegs) {
+          fidx[l] = at + __popc(b & ((1u << lane) - 1u));
+          fkey[l] = buf[l].key;
+        } else {
+          if (fresh) s_list[at + __popc(b & ((1u << lane) - 1u))] = slot;
+        }
       }
     }
 #pragma unroll
@@ -807,6 +819,39 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     __syncthreads();
     const u32 n = s_n;
     const unsigned long long base = s_base;
+    if constexpr (kRegs) {
+#pragma unroll
+      for (int l = 0; l < LPT; ++l)
+        if ((fresh_bits >> l) & 1u) {
+          const u32 slot = slots[l];
+          const u64 key = fkey[l];
+          const u64 idx = base + fidx[l];
+          const bool full = (key & L.mask_of(key)) == L.mask_of(key);
+          if (write_out) keys_out[idx] = key;
+          const u64 folded = kFold ? s_acc[slot] : 0ull;
+          if constexpr (kAcc == 2) {
+            if (write_out) {
+              res_out[idx] = (u32)folded;
+              res_out[out_stride + idx] = (u32)(folded >> 32);
+            }
+            wsum[0] += folded;
+            if (full) fsum[0] += folded;
+          } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              const u32 v = kFold ? reduce_u64(folded, r) : reduce_sum(s_acc[r * H + slot], r);
+              if (write_out) res_out[r * out_stride + idx] = v;
+              wsum[r] += v;
+              if (full) fsum[r] += v;
+            }
+          }
+          s_key[slot] = kEmpty;
+          fstates += full;
+        }
+      (void)n;
+      __syncthreads();
+      continue;
+    }
     for (u32 i = threadIdx.x; i < n; i += BLOCK) {
       const u32 slot = s_list[i];
       const u64 key = s_key[slot];
@@ -1265,9 +1310,16 @@ cudaError_t merge_shape(const PartitionCfg& pc, int blocks_per_sm, const void* r
   if (pc.fold == 2 && !exact) return cudaErrorInvalidValue;  // exact words need the claim-list merge
   if constexpr (Layout::kSlotted)
     if (exact) return cudaErrorInvalidValue;
-  auto kern = fold ? (exact ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, (R == 2 && !Layout::kSlotted) ? 2 : 0>
-                            : partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, R == 2 ? 1 : 0>)
-                   : pc.merge_kind == 1 ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>
+  constexpr bool kRegsOk = !Layout::kSlotted;
+  const bool regs = kRegsOk && pc.merge_regs;
+  auto kern = fold ? (exact ? (regs ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout,
+                                                                  (R == 2 && !Layout::kSlotted) ? 2 : 0, kRegsOk>
+                                    : partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout,
+                                                                  (R == 2 && !Layout::kSlotted) ? 2 : 0>)
+                            : (regs ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, R == 2 ? 1 : 0, kRegsOk>
+                                    : partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, R == 2 ? 1 : 0>))
+                   : pc.merge_kind == 1 ? (regs ? partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout, 0, kRegsOk>
+                                                : partition_merge_list_kernel<R, BLOCK, H, H / 2, Layout>)
                                         : partition_merge_kernel<R, BLOCK, H, H / 2, Layout>;
   const size_t smem = fold ? merge_smem<1, H>() + (size_t)(H / 2) * 4
                            : merge_smem<R, H>() + (pc.merge_kind == 1 ? (size_t)(H / 2) * 4 : 0);

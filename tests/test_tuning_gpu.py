@@ -36,9 +36,10 @@ def tctx(qp):
 @pytest.mark.parametrize("scatter,ppl,merge,wide,fold", [
     combo for combo in itertools.product((0, 1, 2, 3, 4), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
 ])
-def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold):
+@pytest.mark.parametrize("compact", [0, 1])
+def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold, compact):
     tctx.set_tuning(scatter_kind=scatter, parents_per_lane=ppl, merge_kind=merge, wide_merge=wide,
-                    fold_weights=fold)
+                    fold_weights=fold, merge_compact=compact)
     for n in (9, 13):
         got = tctx.contract_rows(n)
         want = _oracle(oracle, n)
@@ -135,7 +136,8 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 
 @pytest.mark.parametrize("field,value", [
-    ("scatter_kind", 5), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3),
+    ("scatter_kind", 5), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3), ("batch_lanes", 0),
+    ("merge_compact", 2), ("unit_target", 100), ("unit_sample", 3),
     ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 3),
 ])
 def test_out_of_range_tuning_is_rejected_and_kept(tctx, qp, field, value):
