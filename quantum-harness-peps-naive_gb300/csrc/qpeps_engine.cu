@@ -294,7 +294,7 @@ struct Ctx {
     uint32_t unit_target = 1000;                // class-grouped partitions: planned candidates per partition
     uint32_t unit_sample = 8;                   // class-grouped partitions: 1 in unit_sample parents sampled
     uint32_t batch_lanes = 2;                   // CUDA-graph replay: device batches run on this many streams
-    uint32_t merge_compact = 1;                 // claim-list merge: 1 = first claimants write from registers
+    uint32_t merge_compact = 0;                 // claim-list merge: 1 = first claimants write from registers
   } tune;
   DevBuf tail;                   // TailControl + overflow list
   DevBuf plan;                   // class-grouped partitions: histogram, bucket table, scan partials
