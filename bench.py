@@ -424,6 +424,17 @@ def run_ours(args):
         if args.same_workload_n:
             line["same_workload"] = same_workload_pair(pkg, ctx, args.same_workload_n, threads)
     ctx.close()
+    if world == 1 and args.dfs_check:
+        # The DFS bitboard oracle (src/dfs_bitmask.rs:67-340, restated in C++)
+        # on all host threads, run in the same job as an independent check.
+        import oracle_py  # noqa: PLC0415
+
+        oracle_py.build()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        dfs = oracle_py.dfs_count(args.n, threads=threads)
+        line["dfs_check"] = {"count": str(dfs), "equal": dfs == results[-1].count, "wall_s": time.perf_counter() - t0,
+                             "threads": threads}
     if world == 1 and args.serve_requests_inline:
         line["serve"] = serve_stream(pkg, args, requests=args.serve_requests_inline, check_nmax=13,
                                      sample_per_n=0, alone_samples=16, compact=True)
@@ -587,9 +598,11 @@ def main():
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dfs-check", action="store_true",
+                    help="after timing, count Q(n) with the CPU DFS bitboard oracle on all host threads")
     ap.add_argument("--same-workload-n", type=int, default=16,
                     help="full Q(n) on both the GPU and the CPU oracle beside the headline (0: skip)")
-    ap.add_argument("--tuning-cache", default=str(ROOT / "profiles" / "tuning_gb300.json"),
+    ap.add_argument("--tuning-cache", default=str(ROOT / PACKAGE / "tuning_gb300.json"),
                     help="autotuner cache (JSON) whose entry for this device and N is applied before timing")
     ap.add_argument("--set-tuning", default="",
                     help="tuning fields applied before timing, e.g. scatter_kind=3,unit_target=1000")

@@ -249,6 +249,11 @@ typedef struct qpeps_tuning {
   uint32_t merge_compact;        /* claim-list merge: 0 (default) = compaction walks a slot list in shared
                                     memory; 1 = a key's first claimant writes the output entry from
                                     registers (exact too; measured about 7 % slower on GB300) */
+  uint32_t scatter_block;        /* one-level scatters: threads per CTA, 128, 256 (default) or 512 */
+  uint32_t merge_auto;           /* what QPEPS_MERGE_AUTO resolves to where both apply:
+                                    QPEPS_MERGE_PARTITION (default) or QPEPS_MERGE_HASH */
+  uint32_t slice_rows;           /* rows enumerated on the host before batching is decided, 1..4 */
+  uint32_t reserved;
 } qpeps_tuning;
 
 /* Library defaults (what a new context starts with). */
@@ -256,10 +261,13 @@ void qpeps_tuning_default(qpeps_tuning* t);
 int qpeps_ctx_get_tuning(void* ctx, qpeps_tuning* out);
 /* QPEPS_ERR_INVALID for an out-of-range field (the context keeps its tuning). */
 int qpeps_ctx_set_tuning(void* ctx, const qpeps_tuning* t, char* err, size_t err_len);
-/* Autotuner: time contract_rows(n) (8 <= n <= 18) under each tuning of a
- * grid over scatter kind, parents per lane, merge kind and partition fill
- * (device time, best of `repeats`; every count checked against
- * known_count), keep the fastest in the context and return it. */
+/* Autotuner: coordinate descent from the context's tuning over scatter kind,
+ * parents per lane, scatter block size, merge kind, merge CTA shape,
+ * partition fill, weight accumulator, merge strategy, batch sizing (slice
+ * margin, host rows) and concurrent batch lanes; each candidate times
+ * contract_rows(n) (8 <= n <= 19) with CUDA-graph replay (device time, best
+ * of `repeats` after a warm-up run; every count checked against known_count).
+ * Keeps the fastest in the context and returns it. */
 int qpeps_autotune(void* ctx, uint32_t n, uint32_t repeats, qpeps_tuning* best, double* best_device_ms, char* err,
                    size_t err_len);
 /* Name of the context's CUDA device (for keying tuning caches). */
@@ -276,10 +284,11 @@ typedef struct qpeps_serve_config {
   uint32_t struct_size;            /* sizeof(qpeps_serve_config) */
   uint32_t max_slots;              /* concurrent requests in the shared batch (<= 64; 0 = 64) */
   uint64_t batch_budget_bytes;     /* device memory of the shared batch (0 = 25 % of free) */
-  uint64_t large_budget_bytes;     /* device memory of the large-request context (0 = 60 % of free) */
+  uint64_t large_budget_bytes;     /* device memory of the large-request contexts together (0 = 60 % of free) */
   uint64_t large_threshold_states; /* estimated peak frontier above which a request runs alone (0 = auto) */
   uint32_t use_cache;              /* 1 = answer repeated (N, prefix or its mirror) from a result cache */
-  uint32_t reserved;
+  uint32_t large_workers;          /* concurrent large-request contexts, each with an equal share of the
+                                      large budget (0 = 2; at most 8) */
 } qpeps_serve_config;
 
 typedef struct qpeps_serve_completion {

@@ -138,7 +138,7 @@ class ServeConfig(ctypes.Structure):
         ("large_budget_bytes", ctypes.c_uint64),
         ("large_threshold_states", ctypes.c_uint64),
         ("use_cache", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("large_workers", ctypes.c_uint32),
     ]
 
 
@@ -200,10 +200,14 @@ class Tuning(ctypes.Structure):
         ("unit_sample", ctypes.c_uint32),
         ("batch_lanes", ctypes.c_uint32),
         ("merge_compact", ctypes.c_uint32),
+        ("scatter_block", ctypes.c_uint32),
+        ("merge_auto", ctypes.c_uint32),
+        ("slice_rows", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "struct_size"}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f not in ("struct_size", "reserved")}
 
 
 # Every symbol include/qpeps.h declares, with its ctypes signature.

@@ -295,6 +295,9 @@ struct Ctx {
     uint32_t unit_sample = 8;                   // class-grouped partitions: 1 in unit_sample parents sampled
     uint32_t batch_lanes = 2;                   // CUDA-graph replay: device batches run on this many streams
     uint32_t merge_compact = 0;                 // claim-list merge: 1 = first claimants write from registers
+    uint32_t scatter_block = 256;               // one-level scatters: threads per CTA (128, 256, 512)
+    uint32_t merge_auto = QPEPS_MERGE_PARTITION;  // what QPEPS_MERGE_AUTO resolves to where both apply
+    uint32_t slice_rows = 1;                    // rows enumerated on the host before slicing is considered
   } tune;
   DevBuf tail;                   // TailControl + overflow list
   DevBuf plan;                   // class-grouped partitions: histogram, bucket table, scan partials
@@ -684,6 +687,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
                     wide, ctx.tune.scatter_kind, ctx.tune.merge_kind,
                     p.w64 ? 2u : (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
     pc.merge_regs = ctx.tune.merge_compact;
+    pc.scatter_block = ctx.tune.scatter_block;
     pc.tl_nb = tl.tl_nb;
     pc.tl_p2 = tl.tl_p2;
     pc.tl_bcap = tl.tl_bcap;
@@ -1110,8 +1114,10 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
     fail(QPEPS_ERR_INVALID, "the partitioned merge needs u64 keys and row granularity");
   if (o.merge == QPEPS_MERGE_HASH)
     p.merge = QPEPS_MERGE_HASH;
-  else if (o.merge == QPEPS_MERGE_PARTITION || o.merge == QPEPS_MERGE_AUTO)
+  else if (o.merge == QPEPS_MERGE_PARTITION)
     p.merge = partition_ok ? QPEPS_MERGE_PARTITION : QPEPS_MERGE_HASH;
+  else if (o.merge == QPEPS_MERGE_AUTO)
+    p.merge = (partition_ok && ctx.tune.merge_auto == QPEPS_MERGE_PARTITION) ? QPEPS_MERGE_PARTITION : QPEPS_MERGE_HASH;
   else
     fail(QPEPS_ERR_INVALID, "unknown merge strategy");
   // The slice tail needs u64 keys and the compiled row operator.
@@ -1825,7 +1831,8 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
   // Seed rows on the host: the first row applies the orbit weights
   // (src/lib.rs:721-749); further rows only when a slice depth is requested.
   const bool orbit = (k == 0) && o.symmetry;
-  const unsigned depth = std::max<unsigned>(o.slice_depth ? o.slice_depth : 1, row0 == 0 ? 1 : row0);
+  const unsigned depth =
+      std::max<unsigned>(o.slice_depth ? o.slice_depth : std::max(1u, ctx.tune.slice_rows), row0 == 0 ? 1 : row0);
   while (row0 < depth && row0 < n) {
     RowAcc& acc = out.rows[row0];
     items = host_expand(n, items, row0, orbit && row0 == 0, acc, out.plan.grain == QPEPS_GRAIN_SITE);
@@ -2047,14 +2054,15 @@ struct Server {
   int device = 0;
   qpeps_serve_config cfg{};
   Ctx* batch = nullptr;
-  Ctx* large = nullptr;
+  std::vector<Ctx*> large;  // one context (own stream, own pool) per large-request worker
   std::mutex mu;
   std::condition_variable cv;
   std::deque<ServeRequest> q_small, q_large;
   std::vector<qpeps_serve_completion> done;
   std::condition_variable cv_done;
   bool stop = false;
-  std::thread t_batch, t_large;
+  std::thread t_batch;
+  std::vector<std::thread> t_large;
   std::map<std::string, u128> cache;
   std::map<std::string, std::vector<ServeWaiter>> inflight;  // queued or running keys (cache on)
   qpeps_serve_stats stats{};
@@ -2352,7 +2360,11 @@ static void serve_batch_loop(Server& sv) {
   }
 }
 
-static void serve_large_loop(Server& sv) {
+// One large-request worker: takes the oldest queued large request and
+// contracts it alone on its own context and stream; several workers overlap
+// their requests on the device, each within an equal share of the large
+// budget, so a long request no longer holds up every other large one.
+static void serve_large_loop(Server& sv, size_t w) {
   cuda_check(cudaSetDevice(sv.device), "cudaSetDevice");
   while (true) {
     ServeRequest r;
@@ -2366,12 +2378,12 @@ static void serve_large_loop(Server& sv) {
     const auto t_admit = ServeClock::now();
     qpeps_options o;
     qpeps_options_default(&o);
-    o.device_budget_bytes = sv.cfg.large_budget_bytes;
+    o.device_budget_bytes = sv.cfg.large_budget_bytes / std::max<size_t>(1, sv.large.size());
     Contraction con;
     int status = QPEPS_OK;
     u128 count = 0;
     try {
-      contract(*sv.large, r.n, o, r.prefix.empty() ? nullptr : r.prefix.data(), (unsigned)r.prefix.size(), con);
+      contract(*sv.large[w], r.n, o, r.prefix.empty() ? nullptr : r.prefix.data(), (unsigned)r.prefix.size(), con);
       count = con.count;
     } catch (const Failure& e) {
       status = e.code;
@@ -2385,10 +2397,10 @@ static void serve_large_loop(Server& sv) {
   }
 }
 
-static void serve_thread_main(Server& sv, bool large) {
+static void serve_thread_main(Server& sv, bool large, size_t w) {
   try {
     if (large)
-      serve_large_loop(sv);
+      serve_large_loop(sv, w);
     else
       serve_batch_loop(sv);
   } catch (const Failure& e) {
@@ -2428,6 +2440,9 @@ static qpeps_tuning tuning_of(const Ctx::Tune& t) {
   q.unit_sample = t.unit_sample;
   q.batch_lanes = t.batch_lanes;
   q.merge_compact = t.merge_compact;
+  q.scatter_block = t.scatter_block;
+  q.merge_auto = t.merge_auto;
+  q.slice_rows = t.slice_rows;
   return q;
 }
 
@@ -2439,6 +2454,11 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
     fail(QPEPS_ERR_INVALID, "unit_sample must be a power of two in [1, 64]");
   if (q.batch_lanes < 1 || q.batch_lanes > 8) fail(QPEPS_ERR_INVALID, "batch_lanes must be in [1, 8]");
   if (q.merge_compact > 1) fail(QPEPS_ERR_INVALID, "merge_compact must be 0 or 1");
+  if (q.scatter_block != 128 && q.scatter_block != 256 && q.scatter_block != 512)
+    fail(QPEPS_ERR_INVALID, "scatter_block must be 128, 256 or 512");
+  if (q.merge_auto != QPEPS_MERGE_PARTITION && q.merge_auto != QPEPS_MERGE_HASH)
+    fail(QPEPS_ERR_INVALID, "merge_auto must be QPEPS_MERGE_PARTITION or QPEPS_MERGE_HASH");
+  if (q.slice_rows < 1 || q.slice_rows > 4) fail(QPEPS_ERR_INVALID, "slice_rows must be in [1, 4]");
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
   if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
@@ -2460,6 +2480,9 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   t.unit_sample = q.unit_sample;
   t.batch_lanes = q.batch_lanes;
   t.merge_compact = q.merge_compact;
+  t.scatter_block = q.scatter_block;
+  t.merge_auto = q.merge_auto;
+  t.slice_rows = q.slice_rows;
   return t;
 }
 
@@ -2468,54 +2491,89 @@ static void apply_tune(Ctx& c, const Ctx::Tune& t) {
   c.partition_fill = t.partition_fill;
 }
 
-// Grid search over the knobs that change the kernels of every row step.
+// Autotuner: coordinate descent over the knobs of a contraction, starting
+// from the context's tuning. Each pass tries, one dimension at a time, every
+// value of that dimension with the others at their best so far and keeps the
+// fastest (device time, best of `repeats` after one untimed warm-up run;
+// every count is checked against known_count); passes repeat until one
+// changes nothing (at most three). A candidate whose warm-up run takes more
+// than three times the best so far is not timed further.
+//   scatter kind, parents per lane, scatter block size, merge kind, merge CTA
+//   shape (wide), partition fill, weight accumulator (fold), merge strategy
+//   (partitioned or global table), batch sizing (slice margin, host rows
+//   before slicing) and concurrent batch lanes.
 static double autotune(Ctx& c, unsigned n, unsigned repeats, Ctx::Tune* best) {
-  if (n < 8 || n > 18) fail(QPEPS_ERR_RANGE, "autotune probe N must be in [8, 18]");
+  if (n < 8 || n > 19) fail(QPEPS_ERR_RANGE, "autotune probe N must be in [8, 19]");
   repeats = std::max(1u, std::min(repeats, 16u));
   u128 known = 0;
   known_count(n, &known);
   qpeps_options o;
   qpeps_options_default(&o);
   o.collect_layers = 0;
+  o.use_graph = 1;  // the timed runs replay the captured contraction, as bench and serving runs do
   const Ctx::Tune saved = c.tune;
+  Ctx::Tune cur = saved;
   double best_ms = 1e300;
-  Ctx::Tune best_t = saved;
+  auto measure = [&](const Ctx::Tune& t, double cap_ms) {
+    apply_tune(c, t);
+    double ms = 1e300;
+    for (unsigned r = 0; r <= repeats; ++r) {
+      Contraction con;
+      contract(c, n, o, nullptr, 0, con);
+      if (con.count != known) fail(QPEPS_ERR_INVALID, "autotune: count differs from known_count");
+      if (r == 0 && con.rs.device_ms > cap_ms) return 1e300;  // far slower than the best: not timed further
+      if (r) ms = std::min(ms, con.rs.device_ms);
+    }
+    return ms;
+  };
+  using Setter = void (*)(Ctx::Tune&, double);
+  struct Dim {
+    std::vector<double> values;
+    Setter set;
+  };
+  const std::vector<Dim> dims = {
+      {{1, 0, 2, 3, 4}, [](Ctx::Tune& t, double v) { t.scatter_kind = (uint32_t)v; }},
+      {{4, 2}, [](Ctx::Tune& t, double v) { t.parents_per_lane = (uint32_t)v; }},
+      {{256, 128, 512}, [](Ctx::Tune& t, double v) { t.scatter_block = (uint32_t)v; }},
+      {{1, 0}, [](Ctx::Tune& t, double v) { t.merge_kind = (uint32_t)v; }},
+      {{2, 0, 1}, [](Ctx::Tune& t, double v) { t.wide_merge = (uint32_t)v; }},
+      {{0.83, 0.9, 0.75}, [](Ctx::Tune& t, double v) { t.partition_fill = v; }},
+      {{2, 1, 0}, [](Ctx::Tune& t, double v) { t.fold_weights = (uint32_t)v; }},
+      {{QPEPS_MERGE_PARTITION, QPEPS_MERGE_HASH}, [](Ctx::Tune& t, double v) { t.merge_auto = (uint32_t)v; }},
+      {{5, 3, 8}, [](Ctx::Tune& t, double v) { t.slice_margin = v; }},
+      {{1, 2}, [](Ctx::Tune& t, double v) { t.slice_rows = (uint32_t)v; }},
+      {{2, 1, 3}, [](Ctx::Tune& t, double v) { t.batch_lanes = (uint32_t)v; }},
+  };
   try {
-    for (uint32_t sk : {1u, 0u, 2u})
-      for (uint32_t ppl : {4u, 2u})
-        for (uint32_t mk : {1u, 0u})
-          for (double fill : {0.83, 0.9, 0.75}) {
-            if (sk == 2 && ppl != 4) continue;  // the two-level scatter has no parents-per-lane knob
-            Ctx::Tune t = saved;
-            t.scatter_kind = sk;
-            t.parents_per_lane = ppl;
-            t.merge_kind = mk;
-            t.partition_fill = fill;
-            apply_tune(c, t);
-            double ms = 1e300;
-            for (unsigned r = 0; r <= repeats; ++r) {  // the first run warms buffers and is not timed
-              Contraction con;
-              contract(c, n, o, nullptr, 0, con);
-              if (con.count != known) fail(QPEPS_ERR_INVALID, "autotune: count differs from known_count");
-              if (r) ms = std::min(ms, con.rs.device_ms);
-            }
-            if (ms < best_ms) {
-              best_ms = ms;
-              best_t = t;
-            }
+    best_ms = measure(cur, 1e300);
+    for (int pass = 0; pass < 3; ++pass) {
+      bool changed = false;
+      for (const Dim& d : dims)
+        for (double v : d.values) {
+          Ctx::Tune t = cur;
+          d.set(t, v);
+          if (std::memcmp(&t, &cur, sizeof t) == 0) continue;
+          const double ms = measure(t, 3.0 * best_ms);
+          if (ms < best_ms) {
+            best_ms = ms;
+            cur = t;
+            changed = true;
           }
+        }
+      if (!changed) break;
+    }
   } catch (...) {
     apply_tune(c, saved);
     throw;
   }
-  apply_tune(c, best_t);
-  *best = best_t;
+  apply_tune(c, cur);
+  *best = cur;
   return best_ms;
 }
 
 extern "C" {
 
-const char* qpeps_version(void) { return "qpeps-gb300 0.1.0 (sm_103a)"; }
+const char* qpeps_version(void) { return "qpeps-gb300 0.2.0 (sm_103a)"; }
 
 void qpeps_options_default(qpeps_options* opt) {
   std::memset(opt, 0, sizeof *opt);
@@ -2669,8 +2727,10 @@ int qpeps_serve_open(int device, const qpeps_serve_config* cfg, void** server_ou
       }
       if (sv->cfg.max_slots == 0 || sv->cfg.max_slots > kServeMaxSlots) sv->cfg.max_slots = kServeMaxSlots;
       sv->device = device;
+      if (sv->cfg.large_workers == 0) sv->cfg.large_workers = 2;
+      if (sv->cfg.large_workers > 8) fail(QPEPS_ERR_INVALID, "large_workers must be at most 8");
       sv->batch = ctx_create(device);
-      sv->large = ctx_create(device);
+      for (uint32_t w = 0; w < sv->cfg.large_workers; ++w) sv->large.push_back(ctx_create(device));
       size_t fr = 0, tot = 0;
       cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
       if (!sv->cfg.batch_budget_bytes) sv->cfg.batch_budget_bytes = (uint64_t)(fr * 0.25);
@@ -2682,11 +2742,20 @@ int qpeps_serve_open(int device, const qpeps_serve_config* cfg, void** server_ou
       if (!sv->cfg.large_threshold_states)
         sv->cfg.large_threshold_states = std::min<uint64_t>(
             16ull << 20, (uint64_t)((double)sv->cfg.batch_budget_bytes / (2.4 * 16.0) / 4.0));
-      sv->t_batch = std::thread(serve_thread_main, std::ref(*sv), false);
-      sv->t_large = std::thread(serve_thread_main, std::ref(*sv), true);
+      sv->t_batch = std::thread(serve_thread_main, std::ref(*sv), false, (size_t)0);
+      for (size_t w = 0; w < sv->large.size(); ++w)
+        sv->t_large.emplace_back(serve_thread_main, std::ref(*sv), true, w);
     } catch (...) {
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+      }
+      sv->cv.notify_all();
+      if (sv->t_batch.joinable()) sv->t_batch.join();
+      for (std::thread& t : sv->t_large)
+        if (t.joinable()) t.join();
       if (sv->batch) ctx_free(sv->batch);
-      if (sv->large) ctx_free(sv->large);
+      for (Ctx* c : sv->large) ctx_free(c);
       delete sv;
       throw;
     }
@@ -2777,13 +2846,14 @@ void qpeps_serve_close(void* server) {
   }
   sv->cv.notify_all();
   if (sv->t_batch.joinable()) sv->t_batch.join();
-  if (sv->t_large.joinable()) sv->t_large.join();
+  for (std::thread& t : sv->t_large)
+    if (t.joinable()) t.join();
   cudaSetDevice(sv->device);
   if (sv->batch) {
     buf_release(*sv->batch, sv->slot_buf);
     ctx_free(sv->batch);
   }
-  if (sv->large) ctx_free(sv->large);
+  for (Ctx* c : sv->large) ctx_free(c);
   delete sv;
 }
 

@@ -118,6 +118,7 @@ struct PartitionCfg {
   uint32_t fold = 0;              // merge_kind 1, R = 2, one 64-bit accumulator plane:
                                   // 1 = CRT-folded residues, 2 = the planes hold an exact weight's
                                   // low and high words (both exact only when N! < p0 * p1, N <= 20)
+  uint32_t scatter_block = 256;   // one-level scatters: threads per CTA (128, 256 or 512; 256 for R > 2)
   uint32_t merge_regs = 0;        // merge_kind 1, fixed layout: first claimants write their entries from
                                   // registers (no slot list in shared memory)
   uint32_t tl_nb = 0;             // two-level scatter: coarse buckets (0 = one-level scatter)

@@ -1270,28 +1270,41 @@ constexpr size_t merge_smem() {
   return (size_t)H * (8 + 8 * R);
 }
 
-template <int R, int PPL, typename Layout>
-cudaError_t scatter_ppl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
-                        u32* cursors, StepScalars* sc, cudaStream_t stream) {
-  u64 want = (n_in + kScatterBlock * PPL - 1) / (kScatterBlock * PPL);
-  const u64 capb = (u64)pc.sms * 8;
+template <int R, int PPL, int BLOCK, typename Layout>
+cudaError_t scatter_shape(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
+                          u32* cursors, StepScalars* sc, cudaStream_t stream) {
+  u64 want = (n_in + BLOCK * PPL - 1) / (BLOCK * PPL);
+  const u64 capb = (u64)pc.sms * 8 * 256 / BLOCK;  // the same resident threads per SM for every block size
   const unsigned grid = (unsigned)std::max<u64>(1, std::min(want, capb));
+  const u32 cstride = pc.cursor_stride ? pc.cursor_stride : 1;
   if (pc.scatter_kind == 4) {
-    partition_scatter_direct_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
+    partition_scatter_direct_kernel<R, BLOCK, PPL, Layout><<<grid, BLOCK, 0, stream>>>(
         reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
-        pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
+        cstride, pc.parts, pc.cap, sc);
     return cudaGetLastError();
   }
   if (pc.scatter_kind != 0) {  // 2 without a two-level plan, or 3 where it does not apply: the window scatter
-    partition_scatter_list_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
+    partition_scatter_list_kernel<R, BLOCK, PPL, Layout><<<grid, BLOCK, 0, stream>>>(
         reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
-        pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
+        cstride, pc.parts, pc.cap, sc);
     return cudaGetLastError();
   }
-  partition_scatter_kernel<R, kScatterBlock, PPL, Layout><<<grid, kScatterBlock, 0, stream>>>(
+  partition_scatter_kernel<R, BLOCK, PPL, Layout><<<grid, BLOCK, 0, stream>>>(
       reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, L, reinterpret_cast<Cand<R>*>(regions), cursors,
-      pc.cursor_stride ? pc.cursor_stride : 1, pc.parts, pc.cap, sc);
+      cstride, pc.parts, pc.cap, sc);
   return cudaGetLastError();
+}
+
+// Block sizes 128 and 512 are instantiated for 16-byte candidates (R <= 2);
+// wider candidates use 256.
+template <int R, int PPL, typename Layout>
+cudaError_t scatter_ppl(const PartitionCfg& pc, const FrontierView& in, u64 n_in, Layout L, void* regions,
+                        u32* cursors, StepScalars* sc, cudaStream_t stream) {
+  if constexpr (R <= 2) {
+    if (pc.scatter_block == 128) return scatter_shape<R, PPL, 128, Layout>(pc, in, n_in, L, regions, cursors, sc, stream);
+    if (pc.scatter_block == 512) return scatter_shape<R, PPL, 512, Layout>(pc, in, n_in, L, regions, cursors, sc, stream);
+  }
+  return scatter_shape<R, PPL, kScatterBlock, Layout>(pc, in, n_in, L, regions, cursors, sc, stream);
 }
 
 template <int R, typename Layout>

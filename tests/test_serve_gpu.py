@@ -137,3 +137,29 @@ def test_identical_requests_in_flight_are_coalesced(qp):
     assert stats["coalesced"] + stats["cache_hits"] == 6
     assert stats["coalesced"] >= 1
     assert {got[t]["path"] for t in range(6)} - {"batch", "large", "cache", "coalesced"} == set()
+
+
+@pytest.mark.parametrize("workers", [1, 3])
+def test_several_large_workers_answer_exactly(qp, oracle, workers):
+    # Large requests run on `workers` contexts at once; every answer equals
+    # the same request contracted alone, whichever worker ran it.
+    reqs = [(14, []), (13, [2]), (14, [5]), (13, []), (14, [1, 8]), (12, [])]
+    with qp.Server(0, use_cache=0, large_threshold_states=20_000, large_workers=workers) as sv:
+        for tag, (n, prefix) in enumerate(reqs):
+            sv.submit(n, prefix, tag)
+        got = {}
+        for _ in range(600):
+            for c in sv.poll(wait_ms=50):
+                got[c["tag"]] = c
+            if len(got) == len(reqs):
+                break
+        stats = sv.stats()
+    assert len(got) == len(reqs)
+    assert stats["large_runs"] >= 4
+    ctx = qp.Context(0)
+    try:
+        for tag, (n, prefix) in enumerate(reqs):
+            assert got[tag]["status"] == 0
+            assert got[tag]["count"] == ctx.count(n, prefix)
+    finally:
+        ctx.close()

@@ -137,7 +137,8 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 @pytest.mark.parametrize("field,value", [
     ("scatter_kind", 5), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3), ("batch_lanes", 0),
-    ("merge_compact", 2), ("unit_target", 100), ("unit_sample", 3),
+    ("merge_compact", 2), ("unit_target", 100), ("unit_sample", 3), ("scatter_block", 300), ("merge_auto", 0),
+    ("slice_rows", 5),
     ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 3),
 ])
 def test_out_of_range_tuning_is_rejected_and_kept(tctx, qp, field, value):
@@ -158,7 +159,9 @@ def test_autotune_picks_a_grid_point_and_caches_it(tctx, qp, tmp_path):
     out = tctx.autotune(n=12, repeats=1, cache=cache)
     assert not out["cached"] and out["device_ms"] > 0
     t = out["tuning"]
-    assert t["scatter_kind"] in (0, 1) and t["parents_per_lane"] in (2, 4) and t["merge_kind"] in (0, 1)
+    assert t["scatter_kind"] in (0, 1, 2, 3, 4) and t["parents_per_lane"] in (2, 4) and t["merge_kind"] in (0, 1)
+    assert t["scatter_block"] in (128, 256, 512) and t["batch_lanes"] in (1, 2, 3) and t["slice_rows"] in (1, 2)
+    assert t["merge_auto"] in (qp.MERGE_PARTITION, qp.MERGE_HASH)
     assert tctx.tuning["scatter_kind"] == t["scatter_kind"]
     entries = json.loads(cache.read_text())
     assert len(entries) == 1 and next(iter(entries)).endswith("|n=12")
@@ -171,9 +174,32 @@ def test_autotune_picks_a_grid_point_and_caches_it(tctx, qp, tmp_path):
         other.close()
 
 
+@pytest.mark.parametrize("block", [128, 512])
+def test_scatter_block_sizes_match_oracle(tctx, qp, oracle, block):
+    for kind in (0, 1, 4):
+        tctx.set_tuning(scatter_block=block, scatter_kind=kind)
+        for n in (9, 13):
+            got = tctx.contract_rows(n)
+            want = _oracle(oracle, n)
+            assert got.count == want["count"]
+            assert [l.output_states for l in got.layers] == [l["output_states"] for l in want["layers"]]
+
+
+def test_merge_auto_and_slice_rows_are_exact(tctx, qp, oracle):
+    tctx.set_tuning(merge_auto=qp.MERGE_HASH)
+    r = tctx.contract_rows(11)
+    assert r.device["merge"] == qp.MERGE_HASH and r.count == qp.known_count(11)
+    tctx.set_tuning(merge_auto=qp.MERGE_PARTITION, slice_rows=2)
+    r = tctx.contract_rows(13)
+    want = _oracle(oracle, 13)
+    assert r.device["merge"] == qp.MERGE_PARTITION and r.count == want["count"]
+    assert r.device["slice_depth"] >= 2
+    assert [l.output_states for l in r.layers] == [l["output_states"] for l in want["layers"]]
+
+
 def test_autotune_rejects_probe_sizes_outside_range(tctx, qp):
     with pytest.raises(qp.ContractionError) as e:
-        tctx.autotune(n=19, repeats=1)
+        tctx.autotune(n=20, repeats=1)
     assert e.value.code == qp.QPEPS_ERR_RANGE
 
 
