@@ -244,8 +244,9 @@ typedef struct qpeps_tuning {
   uint32_t unit_sample;          /* QPEPS_SCATTER_CLASS: 1 in unit_sample parents sampled for the plan
                                     (a power of two, 1..64) */
   uint32_t batch_lanes;          /* CUDA-graph replay: independent device batches run concurrently on
-                                    this many streams, each with its own buffers (1..8; lanes beyond
-                                    the first only while the device budget holds their buffers) */
+                                    this many streams, each with its own buffers (1..8, default 1;
+                                    lanes beyond the first only while the device budget holds their
+                                    buffers, and only with the window or direct scatter) */
   uint32_t merge_compact;        /* claim-list merge: 0 (default) = compaction walks a slot list in shared
                                     memory; 1 = a key's first claimant writes the output entry from
                                     registers (exact too; measured about 7 % slower on GB300) */
@@ -263,8 +264,8 @@ int qpeps_ctx_get_tuning(void* ctx, qpeps_tuning* out);
 int qpeps_ctx_set_tuning(void* ctx, const qpeps_tuning* t, char* err, size_t err_len);
 /* Autotuner: coordinate descent from the context's tuning over scatter kind,
  * parents per lane, scatter block size, merge kind, merge CTA shape,
- * partition fill, weight accumulator, merge strategy, batch sizing (slice
- * margin, host rows) and concurrent batch lanes; each candidate times
+ * partition fill, weight accumulator, merge strategy and batch sizing (slice
+ * margin, host rows); each candidate times
  * contract_rows(n) (8 <= n <= 19) with CUDA-graph replay (device time, best
  * of `repeats` after a warm-up run; every count checked against known_count).
  * Keeps the fastest in the context and returns it. */

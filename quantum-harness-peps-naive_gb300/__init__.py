@@ -552,20 +552,26 @@ class Context:
         return f"{self.device_name}|{version()}|n={int(n)}"
 
     def load_tuning(self, n: int, cache: str | Path) -> dict | None:
-        """Apply the cached autotuner result for this device, library version
-        and ``n`` (no search); returns the cache entry, or None when the cache
-        holds none."""
+        """Apply the cached autotuner result for this device and library
+        version, probed at ``n`` or else at the largest smaller size (no
+        search); returns the cache entry, or None when the cache holds none."""
         import json
 
         try:
             entries = json.loads(Path(cache).read_text())
         except (OSError, ValueError):
             return None
-        e = entries.get(self.tuning_key(n))
-        if e is None:
+        # The entry of this N, else of the largest probe size below it.
+        key = None
+        for m in range(int(n), 7, -1):
+            if self.tuning_key(m) in entries:
+                key = self.tuning_key(m)
+                break
+        if key is None:
             return None
+        e = entries[key]
         self.set_tuning(**e["tuning"])
-        return {"key": self.tuning_key(n), **e}
+        return {"key": key, **e}
 
     def autotune(self, n: int = 16, repeats: int = 2, cache: str | Path | None = None) -> dict:
         """Pick the fastest tuning for this device (``qpeps_autotune`` on a

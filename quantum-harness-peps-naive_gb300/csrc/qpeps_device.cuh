@@ -254,6 +254,7 @@ enum ErrorBits : u32 {
   kErrProbeLimit = 1u,  // hash probe sequence exceeded its bound (table too full)
   kErrOverflow = 2u,    // a bounded structure overflowed its capacity
   kErrWaitLimit = 4u,   // a bounded spin-wait gave up
+  kErrBounds = 8u,      // an index fell outside its buffer; the access was skipped
 };
 
 // Insert one contribution into the global table with linear probing.

@@ -498,6 +498,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   // host's retry with smaller partitions.
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
   unsigned long long wsum[R], fsum[R], fstates = 0;
+  bool bad = false;  // an output index beyond the boundary buffer (skipped)
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
 
@@ -603,11 +604,13 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
         const u64 key = s_key[slot];
         const u64 idx = base + s_cnt[it * WARPS + wid] + __popc(b & ((1u << lane) - 1u));
         const bool full = (key & L.mask_of(key)) == L.mask_of(key);
-        if (write_out) keys_out[idx] = key;
+        const bool wr = write_out && idx < out_stride;
+        bad |= write_out && !wr;
+        if (wr) keys_out[idx] = key;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const u32 v = reduce_sum(s_acc[r * H + slot], r);
-          if (write_out) res_out[r * out_stride + idx] = v;
+          if (wr) res_out[r * out_stride + idx] = v;
           wsum[r] += v;
           if (full) fsum[r] += v;
           s_acc[r * H + slot] = 0ull;
@@ -618,6 +621,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
     }
     __syncthreads();
   }
+  if (bad) atomicOr(&sc->error, kErrBounds);
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     unsigned long long t = pblock_sum<BLOCK>(wsum[r]);
@@ -704,6 +708,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK) s_slot_fin[i] = 0ull;
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
   unsigned long long wsum[R], fsum[R], fstates = 0;
+  bool bad = false;  // an output index beyond the boundary buffer (skipped)
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
   for (int i = threadIdx.x; i < H; i += BLOCK) s_key[i] = kEmpty;
@@ -827,10 +832,12 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
           const u64 key = fkey[l];
           const u64 idx = base + fidx[l];
           const bool full = (key & L.mask_of(key)) == L.mask_of(key);
-          if (write_out) keys_out[idx] = key;
+          const bool wr = write_out && idx < out_stride;
+          bad |= write_out && !wr;
+          if (wr) keys_out[idx] = key;
           const u64 folded = kFold ? s_acc[slot] : 0ull;
           if constexpr (kAcc == 2) {
-            if (write_out) {
+            if (wr) {
               res_out[idx] = (u32)folded;
               res_out[out_stride + idx] = (u32)(folded >> 32);
             }
@@ -840,7 +847,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
 #pragma unroll
             for (int r = 0; r < R; ++r) {
               const u32 v = kFold ? reduce_u64(folded, r) : reduce_sum(s_acc[r * H + slot], r);
-              if (write_out) res_out[r * out_stride + idx] = v;
+              if (wr) res_out[r * out_stride + idx] = v;
               wsum[r] += v;
               if (full) fsum[r] += v;
             }
@@ -857,10 +864,12 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
       const u64 key = s_key[slot];
       const u64 idx = base + i;
       const bool full = (key & L.mask_of(key)) == L.mask_of(key);
-      if (write_out) keys_out[idx] = key;
+      const bool wr = write_out && idx < out_stride;
+      bad |= write_out && !wr;
+      if (wr) keys_out[idx] = key;
       const u64 folded = kFold ? s_acc[slot] : 0ull;
       if constexpr (kAcc == 2) {
-        if (write_out) {
+        if (wr) {
           res_out[idx] = (u32)folded;
           res_out[out_stride + idx] = (u32)(folded >> 32);
         }
@@ -870,7 +879,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const u32 v = kFold ? reduce_u64(folded, r) : reduce_sum(s_acc[r * H + slot], r);
-          if (write_out) res_out[r * out_stride + idx] = v;
+          if (wr) res_out[r * out_stride + idx] = v;
           wsum[r] += v;
           if (full) fsum[r] += v;
         }
@@ -880,6 +889,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     }
     __syncthreads();
   }
+  if (bad) atomicOr(&sc->error, kErrBounds);
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     unsigned long long t = pblock_sum<BLOCK>(wsum[r]);
@@ -1422,6 +1432,7 @@ bool two_level_plan(uint64_t terms, uint32_t parts, int residues, PartitionCfg* 
 cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                      void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
+  if (n_in > in.cap) return cudaErrorInvalidValue;
   if (pc.tl_nb) {
     if (pc.tl_nb > (u32)kTlMaxBins || pc.tl_p2 > (u32)kTlMaxBins || pc.parts != pc.tl_nb * pc.tl_p2)
       return cudaErrorInvalidValue;

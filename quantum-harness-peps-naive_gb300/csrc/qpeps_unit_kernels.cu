@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kUBlock, 2) unit_scatter_kernel(const u64* __r
                                                                   u64 n_in, UnitClassPlan c,
                                                                   const uint2* __restrict__ table,
                                                                   UCand<R>* __restrict__ regions, u32 cap,
-                                                                  u32* __restrict__ cursors, u32 cstride,
+                                                                  u32 units, u32* __restrict__ cursors, u32 cstride,
                                                                   StepScalars* __restrict__ sc) {
   constexpr int BLOCK = kUBlock;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(kUBlock, 2) unit_scatter_kernel(const u64* __r
   constexpr u64 CP = (u64)kUPPT * BLOCK;
   const u64 stride = (u64)gridDim.x * CP;
   const u64 policy = uevict_first_policy();
-  bool overflow = false;
+  bool overflow = false, bounds = false;
 
   u64 ck[kUPPT], cf[kUPPT], nk[kUPPT];
   u32 cw[kUPPT][R], nw[kUPPT][R];
@@ -452,6 +452,11 @@ __global__ void __launch_bounds__(kUBlock, 2) unit_scatter_kernel(const u64* __r
         const u64 key = s_a[i].key;
         const uint2 e = table[ubucket_of(key, c)];
         unit[k] = unit_of(key, e);
+        if (unit[k] >= units) {  // outside the planned partitions: counted as an error, not stored
+          overflow = bounds = true;
+          unit[k] = kFull;
+          continue;
+        }
         u32 slot = (unit[k] * 0x9E3779B1u) >> (32 - 11);
         for (int p = 0; p < 32; ++p) {
           const u32 cur = atomicCAS(&s_mkey[slot], kFull, unit[k]);
@@ -494,7 +499,7 @@ __global__ void __launch_bounds__(kUBlock, 2) unit_scatter_kernel(const u64* __r
       const u32 i = (u32)k * BLOCK + tid;
       bin[k] = kNoBin;
       rank[k] = 0;
-      if (i < m) {
+      if (i < m && unit[k] != kFull) {
         const u32 b = mslot[k] != kFull ? (u32)s_mval[mslot[k]] : kNoBin;
         if (b != kNoBin) {
           bin[k] = b;
@@ -555,6 +560,7 @@ __global__ void __launch_bounds__(kUBlock, 2) unit_scatter_kernel(const u64* __r
     __syncthreads();
   }
   if (overflow) atomicOr(&sc->error, kErrOverflow);
+  if (bounds) atomicOr(&sc->error, kErrBounds);
 }
 
 }  // namespace
@@ -585,6 +591,7 @@ cudaError_t launch_unit_plan(const FrontierView& in, uint64_t n_in, const UnitCl
   UnitPlanTotals* tot = reinterpret_cast<UnitPlanTotals*>(p);
   out->table = table;
   out->totals = tot;
+  if (n_in > in.cap) return cudaErrorInvalidValue;
   if (a.lg > 30 || nblk > 0xffffffffull || a.sample == 0 || (a.sample & (a.sample - 1)) || a.target == 0)
     return cudaErrorInvalidValue;
   if (c.t >= 1 && (a.lg < 3 || c.t > c.n / 2)) return cudaErrorInvalidValue;
@@ -611,6 +618,7 @@ cudaError_t launch_unit_scatter(const PartitionCfg& pc, const FrontierView& in, 
                                 const UnitClassPlan& c, const uint2* table, void* regions, uint32_t* cursors,
                                 StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
+  if (n_in > in.cap) return cudaErrorInvalidValue;
   const u64 chunks = (n_in + (u64)kUPPT * kUBlock - 1) / ((u64)kUPPT * kUBlock);
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(chunks, (u64)pc.sms * 2));
   const u32 cstride = pc.cursor_stride ? pc.cursor_stride : 1;
@@ -620,13 +628,13 @@ cudaError_t launch_unit_scatter(const PartitionCfg& pc, const FrontierView& in, 
     auto k = unit_scatter_kernel<1>;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) return e;
     k<<<grid, kUBlock, smem, stream>>>(reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, c, table,
-                                       reinterpret_cast<UCand<1>*>(regions), pc.cap, cursors, cstride, sc);
+                                       reinterpret_cast<UCand<1>*>(regions), pc.cap, pc.parts, cursors, cstride, sc);
   } else if (pc.residues == 2) {
     constexpr size_t smem = unit_scatter_smem<2>();
     auto k = unit_scatter_kernel<2>;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) return e;
     k<<<grid, kUBlock, smem, stream>>>(reinterpret_cast<const u64*>(in.keys), in.res, in.cap, n_in, c, table,
-                                       reinterpret_cast<UCand<2>*>(regions), pc.cap, cursors, cstride, sc);
+                                       reinterpret_cast<UCand<2>*>(regions), pc.cap, pc.parts, cursors, cstride, sc);
   } else {
     return cudaErrorInvalidValue;
   }

@@ -86,6 +86,8 @@ def test_concurrent_batch_lanes_replay_exactly(gctx, qp, lanes):
 
 
 def test_lanes_with_class_partitions_replay_exactly(gctx, qp):
+    # Class-grouped partitions keep one lane (only the window and direct
+    # scatters run on several); the replay is exact either way.
     gctx.set_tuning(batch_lanes=2, scatter_kind=qp.SCATTER_CLASS)
     budget = 48 << 20
     eager = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
