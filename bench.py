@@ -293,7 +293,8 @@ def run_ours(args):
         opts["granularity"] = pkg.GRAIN_SITE
     if args.tail_row is not None:
         opts["tail_row"] = args.tail_row
-    merged = merged_entries(pkg, args.n, device, opts) if args.grain == "row" else None
+    merged = (merged_entries(pkg, args.n, device, opts)
+              if args.grain == "row" and not args.no_merged_run else None)
     ctx = pkg.Context(device)
     tuning_note = None
     if args.tuning_cache and Path(args.tuning_cache).exists():
@@ -397,6 +398,8 @@ def run_ours(args):
             "tuning_cache": tuning_note,
         },
         "count": str(results[-1].count),
+        **({"layers": [[l.row, l.input_states, l.completed_row_terms, l.output_states] for l in results[-1].layers]}
+           if args.layers else {}),
         "wall_s_per_step": wall_s,
         "device_s_per_step": dev_s,
         "boundary_entries_per_step": entries,
@@ -598,6 +601,10 @@ def main():
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--layers", action="store_true",
+                    help="add each row's [row, input states, successor terms, output states] of the last step")
+    ap.add_argument("--no-merged-run", action="store_true",
+                    help="skip the untimed single-batch contraction that measures the merged entries")
     ap.add_argument("--dfs-check", action="store_true",
                     help="after timing, count Q(n) with the CPU DFS bitboard oracle on all host threads")
     ap.add_argument("--same-workload-n", type=int, default=16,
