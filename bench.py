@@ -60,10 +60,12 @@ sys.path.insert(0, str(ROOT / "oracle"))
 PACKAGE = "quantum-harness-peps-naive_gb300"
 
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# byte of the merge step, from a capture of a few peak-row scatter and merge
-# launches (profiles/); the bench scales the contraction's algorithmic bytes
-# by it. Keyed by the scatter kind the figure was captured with.
-TRAFFIC_PER_ALGORITHMIC_BYTE: dict = {}
+# byte of the merge step, from a capture of the scatter and merge launches of
+# rows 11-13 of Q(17) (the peak rows; profiles/dram_q17_peak_rows.md): 171.29 GB
+# moved for 56.97 GB of algorithmic bytes. The bench scales the contraction's
+# algorithmic bytes by it (an upper estimate: the peak rows re-read the most).
+# Keyed by the scatter kind the figure was captured with (1, the window scatter).
+TRAFFIC_PER_ALGORITHMIC_BYTE: dict = {1: 171.290302464 / 56.96632816}
 METRIC = "Q(N) wall time & boundary entries/s at N=18 (bit-exact)"
 UNIT = "boundary entries/s"
 
@@ -360,8 +362,9 @@ def run_ours(args):
         "unit": "GB/s",
         "frac": achieved / peak,
         "traffic": (tpb * d["merge_kernel_bytes"]) if tpb else None,
-        "traffic_scope": ("DRAM bytes per step, scaled from the DRAM bytes per algorithmic byte of an ncu capture of "
-                          "peak-row scatter and merge launches" if tpb else "no capture for this configuration"),
+        "traffic_scope": ("DRAM bytes per step: the step's algorithmic bytes x 3.007, the DRAM bytes per algorithmic "
+                          "byte that ncu measured on the scatter and merge launches of Q(17) rows 11-13 (an upper "
+                          "estimate)" if tpb else "no capture for this configuration"),
         "algorithmic_bytes_per_step": d["merge_kernel_bytes"],
         "launches_per_step": d["merge_kernel_launches"],
         "scatter_ms_per_step": d["scatter_kernel_ms"],
