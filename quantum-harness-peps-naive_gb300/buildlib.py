@@ -33,8 +33,8 @@ NVCC_FLAGS = ARCH + [
     "-I",
     str(INCLUDE),
 ]
-LIB_SOURCES = ["qpeps_hash_kernels.cu", "qpeps_partition_kernels.cu", "qpeps_unit_kernels.cu", "qpeps_engine.cu",
-               "qpeps_noalloc.cu", "qpeps_tail_kernels.cu"]
+LIB_SOURCES = ["qpeps_hash_kernels.cu", "qpeps_partition_kernels.cu", "qpeps_unit_kernels.cu", "qpeps_wide_kernels.cu",
+               "qpeps_engine.cu", "qpeps_noalloc.cu", "qpeps_tail_kernels.cu"]
 
 
 def nvcc() -> str:

@@ -422,6 +422,8 @@ struct Plan {
 };
 
 static size_t entry_bytes(const Plan& p) { return (size_t)(p.key_bits / 8) + 4u * p.R; }
+// Bytes of one partitioned-merge candidate (key and residue words, padded).
+static size_t cand_bytes(const Plan& p) { return p.key_bits == 128 ? 32 : candidate_bytes(p.R); }
 
 static FrontierView view_of(const Plan& p, DevBuf& b, u64 cap) {
   FrontierView v;
@@ -511,7 +513,7 @@ static bool ensure_front(Ctx& ctx, const Plan& p, DevFrontier& f, u64 need, size
   const size_t eb = entry_bytes(p);
   // Grow in large steps (x3, capped where the step's scratch would no longer
   // fit next to the boundary) so that a growing frontier is copied rarely.
-  const u64 step_cap = (u64)((double)p.budget / ((double)eb + 1.25 * (double)candidate_bytes(p.R)));
+  const u64 step_cap = (u64)((double)p.budget / ((double)eb + 1.25 * (double)cand_bytes(p)));
   u64 want = std::max<u64>(need, std::min<u64>(need * 3, step_cap));
   const size_t live = ctx.front[0].bytes;
   if (live + want * eb + other_bytes > p.budget) want = need;
@@ -605,9 +607,11 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   const bool want_wide = ctx.tune.wide_merge == 1 ||
                          (ctx.tune.wide_merge == 2 && narrow_parts > (double)ctx.tune.wide_above_parts);
   // Class-grouped partitions (16-byte candidates, narrow merge CTAs).
-  const bool unit = partition && ctx.tune.scatter_kind == 3 && unit_scatter_supported(p.R);
-  const u32 wide = (!unit && want_wide && wide_merge_supported(p.R)) ? 1u : 0u;
-  const u32 pcap = partition_capacity(wide);
+  // 128-bit keys: their own scatter and merge (one shape, 1024-candidate partitions).
+  const bool wkeys = p.key_bits == 128;
+  const bool unit = partition && !wkeys && ctx.tune.scatter_kind == 3 && unit_scatter_supported(p.R);
+  const u32 wide = (!unit && !wkeys && want_wide && wide_merge_supported(p.R)) ? 1u : 0u;
+  const u32 pcap = wkeys ? wide_key_partition_capacity() : partition_capacity(wide);
   double mean = ctx.partition_fill * pcap;
   double unit_target = ctx.tune.unit_target;
   for (int attempt = 0;; ++attempt) {
@@ -644,15 +648,15 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
       if (tot.units == 0 || tot.units > 0xffffffffull)
         fail(QPEPS_ERR_CAPACITY, row_msg("partition plan out of range at row", row + 1));
       parts = (u32)tot.units;
-      region_bytes = (size_t)parts * pcap * candidate_bytes(p.R);
+      region_bytes = (size_t)parts * pcap * cand_bytes(p);
       cstride = (parts <= ctx.tune.spread_cursors_below) ? 8u : 1u;
       table_bytes = region_bytes + ((size_t)parts * 4 * cstride + 255) / 256 * 256;
     } else if (partition) {
       const u64 parts64 = std::max<u64>(1, (u64)((double)so.terms / mean) + 1);
       if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, row_msg("too many partitions at row", row + 1));
       parts = (u32)parts64;
-      if (ctx.tune.scatter_kind == 2 && two_level_plan(so.terms, parts, p.R, &tl)) parts = tl.parts;
-      region_bytes = (size_t)parts * pcap * candidate_bytes(p.R);
+      if (!wkeys && ctx.tune.scatter_kind == 2 && two_level_plan(so.terms, parts, p.R, &tl)) parts = tl.parts;
+      region_bytes = (size_t)parts * pcap * cand_bytes(p);
       cstride = (parts <= ctx.tune.spread_cursors_below) ? 8u : 1u;
       table_bytes = region_bytes + ((size_t)parts * 4 * cstride + 255) / 256 * 256;
       if (tl.tl_nb) {
@@ -688,6 +692,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
                     p.w64 ? 2u : (ctx.tune.fold_weights && p.R == 2 && p.free_rows <= 20) ? 1u : 0u};
     pc.merge_regs = ctx.tune.merge_compact;
     pc.scatter_block = ctx.tune.scatter_block;
+    pc.key_bits = (uint32_t)p.key_bits;
     pc.tl_nb = tl.tl_nb;
     pc.tl_p2 = tl.tl_p2;
     pc.tl_bcap = tl.tl_bcap;
@@ -1111,9 +1116,9 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
     p.budget = (size_t)((double)(fr + ctx.pool_bytes) * 0.90);
   }
   p.threads = o.block_threads ? (int)o.block_threads : 256;
-  const bool partition_ok = p.key_bits == 64 && p.grain == QPEPS_GRAIN_ROW;
+  const bool partition_ok = (p.key_bits == 64 || p.key_bits == 128) && p.grain == QPEPS_GRAIN_ROW;
   if (o.merge == QPEPS_MERGE_PARTITION && !partition_ok)
-    fail(QPEPS_ERR_INVALID, "the partitioned merge needs u64 keys and row granularity");
+    fail(QPEPS_ERR_INVALID, "the partitioned merge needs row granularity");
   if (o.merge == QPEPS_MERGE_HASH)
     p.merge = QPEPS_MERGE_HASH;
   else if (o.merge == QPEPS_MERGE_PARTITION)
@@ -1510,7 +1515,7 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
   graph_free(ctx);
   const Plan& p = done.plan;
   if (!rec.ok || rec.chunks.empty() || p.merge != QPEPS_MERGE_PARTITION || p.grain != QPEPS_GRAIN_ROW ||
-      p.key_bits != 64 || !ctx.front[0].ptr || !ctx.table.ptr)
+      !ctx.front[0].ptr || !ctx.table.ptr)
     return;
   const size_t eb = entry_bytes(p), kb = key_bytes(p);
   const u64 cap0 = ctx.front[0].bytes / eb;
@@ -1866,7 +1871,7 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
   // deeper prefix slices) one chunk at a time instead of halving a live
   // frontier at its peak and spilling it to the host.
   if (o.slice_depth == 0 && out.plan.grain == QPEPS_GRAIN_ROW && row0 < n && !items.empty()) {
-    const double per_state = 2.0 * (double)entry_bytes(out.plan) + 1.25 * (double)candidate_bytes(out.plan.R);
+    const double per_state = 2.0 * (double)entry_bytes(out.plan) + 1.25 * (double)cand_bytes(out.plan);
     const double cap_states = 0.8 * (double)out.plan.budget / per_state;
     double est_total = serve_estimate(n, k);
     while (est_total > cap_states && row0 + 2 < n) {

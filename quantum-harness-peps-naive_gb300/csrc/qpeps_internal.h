@@ -118,6 +118,7 @@ struct PartitionCfg {
   uint32_t fold = 0;              // merge_kind 1, R = 2, one 64-bit accumulator plane:
                                   // 1 = CRT-folded residues, 2 = the planes hold an exact weight's
                                   // low and high words (both exact only when N! < p0 * p1, N <= 20)
+  uint32_t key_bits = 64;         // 128: wide-key scatter and merge (32-byte candidates, `cap` = 1024)
   uint32_t scatter_block = 256;   // one-level scatters: threads per CTA (128, 256 or 512; 256 for R > 2)
   uint32_t merge_regs = 0;        // merge_kind 1, fixed layout: first claimants write their entries from
                                   // registers (no slot list in shared memory)
@@ -127,6 +128,15 @@ struct PartitionCfg {
 };
 
 size_t candidate_bytes(int residues);
+// Partitioned merge with 128-bit keys: candidate slots per partition (1024),
+// and its scatter and merge (window scatter; claim-list merge over residue
+// planes with a 2048-slot table of 128-bit keys).
+uint32_t wide_key_partition_capacity();
+cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
+                                          void* regions, uint32_t* cursors, StepScalars* scalars, cudaStream_t stream);
+cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
+                                        const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
+                                        cudaStream_t stream);
 // Candidate slots per partition for a merge shape (PartitionCfg::wide).
 uint32_t partition_capacity(uint32_t wide = 0);
 // Whether the wide merge shape is available for a residue count.

@@ -1433,6 +1433,7 @@ cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView&
                                      void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
   if (n_in > in.cap) return cudaErrorInvalidValue;
+  if (pc.key_bits == 128) return launch_wide_partition_scatter(pc, in, n_in, n, regions, cursors, sc, stream);
   if (pc.tl_nb) {
     if (pc.tl_nb > (u32)kTlMaxBins || pc.tl_p2 > (u32)kTlMaxBins || pc.parts != pc.tl_nb * pc.tl_p2)
       return cudaErrorInvalidValue;
@@ -1453,6 +1454,7 @@ cudaError_t launch_partition_scatter(const PartitionCfg& pc, const FrontierView&
 cudaError_t launch_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                    const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
                                    cudaStream_t stream) {
+  if (pc.key_bits == 128) return launch_wide_partition_merge(pc, regions, cursors, out, n, write_out, sc, stream);
   switch (pc.residues) {
     case 1: return merge_impl<1>(pc, regions, cursors, out, FixedLayout{n, pboard_mask_host(n)}, write_out, sc, stream);
     case 2: return merge_impl<2>(pc, regions, cursors, out, FixedLayout{n, pboard_mask_host(n)}, write_out, sc, stream);

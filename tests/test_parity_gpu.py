@@ -158,9 +158,10 @@ def _legal_prefix(n, k, seed):
 
 @pytest.mark.parametrize("n,k", [(22, 7), (24, 9), (26, 11), (28, 13), (30, 15), (42, 30)])
 def test_boards_beyond_u64_keys_use_u128_keys_and_match_oracle(ctx, oracle, n, k):
-    # N >= 22: the packed boundary needs 3N > 64 bits, so keys are u128 and
-    # the merge is the global table (natural, not forced); N = 42 is the
-    # widest board the reference accepts. The
+    # N >= 22: the packed boundary needs 3N > 64 bits, so keys are u128 (natural,
+    # not forced) and the merge is the partitioned one with 128-bit keys; the
+    # global table gives the same count. N = 42 is the widest board the
+    # reference accepts. The
     # prefixes keep the oracle's frontier at up to about 0.4 M states.
     prefix = _legal_prefix(n, k, 1000 + n)
     count, res = ctx.count_with_stats(n, prefix)
@@ -176,6 +177,40 @@ def test_boards_beyond_u64_keys_use_u128_keys_and_match_oracle(ctx, oracle, n, k
     want = oracle.contract(n, backend=oracle.PARALLEL_SORT_REDUCE, threads=8, symmetry=False, prefix=prefix)
     assert count == want["count"]
     assert res.peak_states == want["peak_states"]
+
+
+@pytest.mark.parametrize("n", [13, 15, 16])
+def test_wide_key_partitioned_merge_equals_global_table(ctx, qp, n):
+    # 128-bit keys forced: the partitioned scatter and merge with 32-byte
+    # candidates give the global table's frontier row by row, and the
+    # default u64 path's; a CUDA-graph replay of it is exact too.
+    part = ctx.contract_rows(n, key_bits=128, merge=qp.MERGE_PARTITION)
+    table = ctx.contract_rows(n, key_bits=128, merge=qp.MERGE_HASH)
+    narrow = ctx.contract_rows(n)
+    assert part.device["merge"] == qp.MERGE_PARTITION and part.device["key_bits"] == 128
+    assert part.count == table.count == narrow.count == qp.known_count(n)
+    assert _gpu_layers(part) == _gpu_layers(table) == _gpu_layers(narrow)
+    first = ctx.contract_rows(n, key_bits=128, use_graph=1)
+    again = ctx.contract_rows(n, key_bits=128, use_graph=1)
+    assert again.device["gpu_launches"] < first.device["gpu_launches"]
+    assert _gpu_layers(again) == _gpu_layers(narrow) and again.count == narrow.count
+
+
+@pytest.mark.parametrize("residues", [1, 3, 4])
+def test_wide_key_partitioned_merge_residue_planes(ctx, oracle, residues):
+    n = 11 if residues == 1 else 12
+    g = ctx.contract_rows(n, key_bits=128, residues=residues)
+    assert g.device["residues"] == residues and g.device["key_bits"] == 128
+    assert g.count == oracle.known_count(n)
+    assert _gpu_layers(g) == _oracle_layers(oracle.contract(n))
+
+
+def test_wide_key_partitioned_merge_wide_boards_both_merges(ctx, qp, oracle):
+    prefix = _legal_prefix(24, 10, 77)
+    a = ctx.count(24, prefix, merge=qp.MERGE_PARTITION)
+    b = ctx.count(24, prefix, merge=qp.MERGE_HASH)
+    want = oracle.contract(24, backend=oracle.PARALLEL_SORT_REDUCE, threads=8, symmetry=False, prefix=prefix)
+    assert a == b == want["count"]
 
 
 @pytest.mark.parametrize("residues", [1, 2, 3, 4])
@@ -267,9 +302,9 @@ def test_both_merge_strategies_match_oracle(ctx, oracle, qp, n, merge):
     assert _gpu_layers(g) == _oracle_layers(o)
 
 
-def test_partition_merge_is_default_for_u64_keys(ctx, qp):
+def test_partition_merge_is_default_for_row_grain(ctx, qp):
     assert ctx.contract_rows(12).device["merge"] == qp.MERGE_PARTITION
-    assert ctx.contract_rows(12, key_bits=128).device["merge"] == qp.MERGE_HASH
+    assert ctx.contract_rows(12, key_bits=128).device["merge"] == qp.MERGE_PARTITION
     assert ctx.contract_rows(9, granularity=1).device["merge"] == qp.MERGE_HASH
     with pytest.raises(qp.ContractionError):
         ctx.contract_rows(9, granularity=1, merge=qp.MERGE_PARTITION)
