@@ -422,7 +422,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         lib = library()
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         h = _VP()
         _check(lib.qpeps_ctx_create(device, ctypes.byref(h), err, len(err)), err)
         self._h = h
@@ -446,7 +446,7 @@ class Context:
         res = Result()
         cap = max(int(n), 1)
         layers = (Layer * cap)()
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         with self._lock:
             rc = lib.qpeps_contract_rows(self._h, int(n), ctypes.byref(o), ctypes.byref(res), layers, cap, err, len(err))
         _check(rc, err)
@@ -464,7 +464,7 @@ class Context:
         arr = (ctypes.c_uint32 * max(k, 1))(*prefix)
         out = U128()
         res = Result()
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         with self._lock:
             rc = lib.qpeps_count(self._h, int(n), arr if k else None, k, ctypes.byref(o), ctypes.byref(out),
                                  ctypes.byref(res), err, len(err))
@@ -486,7 +486,7 @@ class Context:
         pc = (ctypes.c_uint32 * max(len(cols), 1))(*cols)
         counts = (U128 * max(num, 1))()
         o = options(**opts)
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         with self._lock:
             rc = lib.qpeps_count_batch(self._h, num, ns, ks, po, pc, ctypes.byref(o), counts, err, len(err))
         _check(rc, err)
@@ -497,7 +497,7 @@ class Context:
         """Replaces ``contract_explicit_c_frontier(n, order, support_limit)``
         (src/lib.rs:961-967); ``count`` is None when the result is incomplete."""
         out = ExplicitResult()
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         with self._lock:
             rc = library().qpeps_explicit_frontier(self._h, int(n), int(order), int(support_limit), ctypes.byref(out),
                                                    err, len(err))
@@ -535,7 +535,7 @@ class Context:
             if k not in t.as_dict():
                 raise ContractionError(QPEPS_ERR_INVALID, f"unknown tuning field {k}")
             setattr(t, k, v)
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         with self._lock:
             rc = library().qpeps_ctx_set_tuning(self._h, ctypes.byref(t), err, len(err))
         _check(rc, err)
@@ -594,7 +594,7 @@ class Context:
                 return {"tuning": self.tuning, "device_ms": entries[key]["device_ms"], "cached": True}
         t = Tuning()
         ms = ctypes.c_double()
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         with self._lock:
             rc = library().qpeps_autotune(self._h, int(n), int(repeats), ctypes.byref(t), ctypes.byref(ms), err,
                                           len(err))
@@ -626,7 +626,7 @@ class Server:
             if not hasattr(c, k) or k == "struct_size":
                 raise TypeError(f"unknown serve option {k}")
             setattr(c, k, int(v))
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         h = _VP()
         _check(lib.qpeps_serve_open(device, ctypes.byref(c), ctypes.byref(h), err, len(err)), err)
         self._h = h
@@ -634,7 +634,7 @@ class Server:
     def submit(self, n: int, prefix: Sequence[int] = (), tag: int = 0) -> None:
         k = len(prefix)
         arr = (ctypes.c_uint32 * max(k, 1))(*prefix)
-        err = ctypes.create_string_buffer(512)
+        err = ctypes.create_string_buffer(4096)
         _check(library().qpeps_serve_submit(self._h, n, arr if k else None, k, tag, err, len(err)), err)
 
     def poll(self, max_items: int = 1024, wait_ms: int = 0) -> list[dict]:
@@ -647,7 +647,7 @@ class Server:
             for b in buf[: got.value]
         ]
         if rc != QPEPS_OK:
-            err = ctypes.create_string_buffer(512)
+            err = ctypes.create_string_buffer(4096)
             code = library().qpeps_serve_error(self._h, err, len(err))
             raise ContractionError(code or rc, "server stopped: " + err.value.decode(errors="replace"))
         return out
@@ -722,7 +722,7 @@ def certify_c(entries: Sequence[tuple[int, int]]) -> None:
     m = len(entries)
     legs = (ctypes.c_uint32 * max(m, 1))(*[e[0] for e in entries])
     vals = (ctypes.c_uint64 * max(m, 1))(*[e[1] for e in entries])
-    err = ctypes.create_string_buffer(512)
+    err = ctypes.create_string_buffer(4096)
     _check(lib.qpeps_certify_c(legs, vals, m, err, len(err)), err)
 
 

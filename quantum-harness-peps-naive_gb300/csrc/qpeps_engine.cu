@@ -1541,15 +1541,24 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
   }
   // Lanes: whole batches, heaviest first to the least loaded lane; a lane
   // beyond the first is kept only while the device budget holds its buffers.
-  // Several lanes are used only with the window and direct scatters (the
-  // combinations run and checked at Q(18) on GB300); an autotuning run that
-  // replayed Q(18) on two lanes with one of the other scatter kinds stopped on
-  // an illegal address that reading the code has not explained, so those
-  // kinds keep one lane.
+  // Several lanes are used only with the window and direct scatters, the
+  // combinations run and checked at Q(18) on GB300. (An autotuning run that
+  // replayed Q(18) on two lanes stopped on an illegal address; the likely
+  // cause is the class-grouped replay described below, which wrote through
+  // partition indices beyond its regions before the bounds check existed.)
   bool lanes_ok = true;
   for (const GraphChunkRec& c : rec.chunks)
     for (const GraphStepRec& st : c.steps)
       if (st.terms && st.pc.scatter_kind != 1 && st.pc.scatter_kind != 4) lanes_ok = false;
+  // Class-grouped partitions are not captured: in one replay of Q(17) the plan
+  // rebuilt on the device at a later row named more partitions than the
+  // recorded run had (caught by the class scatter's bounds check, the access
+  // skipped), so an earlier replayed row had left a different boundary; the
+  // cause is not found. Those contractions run eagerly, where every row's
+  // plan is read back before its scatter.
+  for (const GraphChunkRec& c : rec.chunks)
+    for (const GraphStepRec& st : c.steps)
+      if (st.terms && st.unit) return;
   unsigned nl = lanes_ok ? (unsigned)std::max<u64>(1, std::min<u64>(ctx.tune.batch_lanes, nc)) : 1u;
   std::vector<size_t> order(nc);
   for (size_t i = 0; i < nc; ++i) order[i] = i;
@@ -1692,7 +1701,7 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
             // The plan is a function of the boundary's keys only: the replay
             // rebuilds the recorded one.
             UnitPlanDev upd{};
-            ok(launch_unit_plan(view, st.n_in, st.ucp, st.upa, L.plan.ptr, ctx.sms, st_, &upd));
+            ok(launch_unit_plan(view, st.n_in, st.ucp, st.upa, L.plan.ptr, ctx.sms, st_, &upd, sc));
             ok(launch_unit_scatter(st.pc, view, st.n_in, st.ucp, upd.table, regions, cursors, sc, st_));
             g->launches += 4;
           } else {
@@ -1748,18 +1757,25 @@ static bool graph_replay(Ctx& ctx, unsigned n, const qpeps_options& o, const uin
   const int R = g->base.plan.R;
   size_t si = 0;
   bool same = true;
+  std::string trail;  // per step: recorded / replayed output entries and plan units, error bits
   for (size_t ci = 0; ci < g->chunks.size(); ++ci)
     for (size_t sj = 0; sj < g->chunks[ci].steps.size(); ++sj) {
       const GraphStepRec& st = g->chunks[ci].steps[sj];
       const StepScalars& h = g->h_scal[si++];
+      if (st.terms && trail.size() < 1500) {
+        char buf[128];
+        std::snprintf(buf, sizeof buf, " [%zu.%zu out %llu/%llu units %u/%llu err %u]", ci, sj,
+                      (unsigned long long)st.out, h.out_count, st.pc.parts, h.plan_units, h.error);
+        trail += buf;
+      }
       if (h.error & kErrBounds) {
-        char msg[160];
+        char msg[200];
         std::snprintf(msg, sizeof msg,
                       "a kernel's bounds check failed (access skipped) in the graph replay, batch %zu step %zu "
-                      "(scatter kind %u, %u partitions)",
+                      "(scatter kind %u, %u partitions); steps:",
                       ci, sj, st.pc.scatter_kind, st.pc.parts);
         graph_free(ctx);
-        fail(QPEPS_ERR_CUDA, msg);
+        fail(QPEPS_ERR_CUDA, std::string(msg) + trail);
       }
       if (!st.terms) continue;
       same = same && h.error == 0 && h.out_count == st.out;
@@ -2524,7 +2540,8 @@ static void apply_tune(Ctx& c, const Ctx::Tune& t) {
 // every count is checked against known_count); passes repeat until one
 // changes nothing (at most three). A candidate whose warm-up run takes more
 // than three times the best so far is not timed further.
-//   scatter kind, parents per lane, scatter block size, merge kind, merge CTA
+//   scatter kind (not the class-grouped one, which is not graph-captured),
+//   parents per lane, scatter block size, merge kind, merge CTA
 //   shape (wide), partition fill, weight accumulator (fold), merge strategy
 //   (partitioned or global table) and batch sizing (slice margin, host rows
 //   before slicing). Concurrent batch lanes are left as set (graph_build).
@@ -2558,7 +2575,7 @@ static double autotune(Ctx& c, unsigned n, unsigned repeats, Ctx::Tune* best) {
     Setter set;
   };
   const std::vector<Dim> dims = {
-      {{1, 0, 2, 3, 4}, [](Ctx::Tune& t, double v) { t.scatter_kind = (uint32_t)v; }},
+      {{1, 0, 2, 4}, [](Ctx::Tune& t, double v) { t.scatter_kind = (uint32_t)v; }},
       {{4, 2}, [](Ctx::Tune& t, double v) { t.parents_per_lane = (uint32_t)v; }},
       {{256, 128, 512}, [](Ctx::Tune& t, double v) { t.scatter_block = (uint32_t)v; }},
       {{1, 0}, [](Ctx::Tune& t, double v) { t.merge_kind = (uint32_t)v; }},

@@ -37,7 +37,8 @@ struct StepScalars {
   unsigned int pad0;
   unsigned long long sitewise_examined;  // row count: C entries the reference's per-parent sitewise
                                          // row kernel matches over the input (sitewise_entries())
-  unsigned int pad[4];
+  unsigned long long plan_units;         // class-grouped partitions: units of the step's plan (graph replay)
+  unsigned int pad[2];
 };
 
 struct LaunchCfg {
@@ -186,7 +187,8 @@ size_t unit_plan_scratch_bytes(uint32_t lg);
 // Sampled histogram of the step's successors and the bucket -> units table;
 // the unit count lands in out->totals (device) for the host to read.
 cudaError_t launch_unit_plan(const FrontierView& in, uint64_t n_in, const UnitClassPlan& c, const UnitPlanArgs& a,
-                             void* scratch, int sms, cudaStream_t stream, UnitPlanDev* out);
+                             void* scratch, int sms, cudaStream_t stream, UnitPlanDev* out,
+                             StepScalars* scalars = nullptr);
 cudaError_t launch_unit_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in,
                                 const UnitClassPlan& c, const uint2* table, void* regions, uint32_t* cursors,
                                 StepScalars* scalars, cudaStream_t stream);

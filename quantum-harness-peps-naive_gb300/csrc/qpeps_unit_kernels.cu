@@ -200,7 +200,8 @@ __global__ void __launch_bounds__(kPlanBlock) unit_plan_sums_kernel(const u32* _
 
 // One CTA: exclusive scans of the block sums (in place) and the totals.
 __global__ void __launch_bounds__(1024) unit_plan_scan_kernel(u64* __restrict__ block_small, u64* __restrict__ block_own,
-                                                              u32 nblocks, UnitPlanArgs a, UnitPlanTotals* __restrict__ tot) {
+                                                              u32 nblocks, UnitPlanArgs a, UnitPlanTotals* __restrict__ tot,
+                                                              StepScalars* __restrict__ sc) {
   __shared__ u64 s_warp[32];
   u64 carry_s = 0, carry_o = 0;
   for (u32 base = 0; base < nblocks; base += 1024) {
@@ -228,6 +229,7 @@ __global__ void __launch_bounds__(1024) unit_plan_scan_kernel(u64* __restrict__ 
     tot->small_units = small_units;
     tot->units = small_units + carry_o;
     tot->small_e = carry_s;
+    if (sc) sc->plan_units = small_units + carry_o;
   }
 }
 
@@ -575,7 +577,7 @@ size_t unit_plan_scratch_bytes(uint32_t lg) {
 }
 
 cudaError_t launch_unit_plan(const FrontierView& in, uint64_t n_in, const UnitClassPlan& c, const UnitPlanArgs& a,
-                             void* scratch, int sms, cudaStream_t stream, UnitPlanDev* out) {
+                             void* scratch, int sms, cudaStream_t stream, UnitPlanDev* out, StepScalars* sc) {
   const size_t nb = (size_t)1 << a.lg;
   const size_t nblk = (nb + kPlanBlock - 1) / kPlanBlock;
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
@@ -608,7 +610,7 @@ cudaError_t launch_unit_plan(const FrontierView& in, uint64_t n_in, const UnitCl
   }
   unit_plan_sums_kernel<<<(unsigned)nblk, kPlanBlock, 0, stream>>>(hist, a, bsmall, bown);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  unit_plan_scan_kernel<<<1, 1024, 0, stream>>>(bsmall, bown, (u32)nblk, a, tot);
+  unit_plan_scan_kernel<<<1, 1024, 0, stream>>>(bsmall, bown, (u32)nblk, a, tot, sc);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   unit_plan_table_kernel<<<(unsigned)nblk, kPlanBlock, 0, stream>>>(hist, a, bsmall, bown, tot, table);
   return cudaGetLastError();

@@ -85,13 +85,13 @@ def test_concurrent_batch_lanes_replay_exactly(gctx, qp, lanes):
     assert _metrics(replay) == _metrics(eager) == _metrics(again)
 
 
-def test_lanes_with_class_partitions_replay_exactly(gctx, qp):
-    # Class-grouped partitions keep one lane (only the window and direct
-    # scatters run on several); the replay is exact either way.
+def test_class_partitions_are_not_captured(gctx, qp):
+    # Class-grouped partitions run eagerly even with use_graph (they are not
+    # captured); repeated contractions stay exact.
     gctx.set_tuning(batch_lanes=2, scatter_kind=qp.SCATTER_CLASS)
     budget = 48 << 20
     eager = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
-    replay = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
-    assert replay.device["gpu_launches"] < eager.device["gpu_launches"]
-    assert eager.count == replay.count == qp.known_count(15)
-    assert _metrics(replay) == _metrics(eager)
+    again = gctx.contract_rows(15, use_graph=1, device_budget_bytes=budget)
+    assert again.device["gpu_launches"] == eager.device["gpu_launches"]
+    assert eager.count == again.count == qp.known_count(15)
+    assert _metrics(again) == _metrics(eager)

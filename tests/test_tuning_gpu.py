@@ -58,9 +58,10 @@ def test_class_scatter_equals_the_window_scatter(tctx, qp, n):
     assert got.count == ref.count == qp.known_count(n)
     assert _layers(got) == _layers(ref)
     assert got.peak_states == ref.peak_states
+    # Not graph-captured: repeated contractions run eagerly, exact each time.
     first = tctx.contract_rows(n, use_graph=1)
     again = tctx.contract_rows(n, use_graph=1)
-    assert again.device["gpu_launches"] < first.device["gpu_launches"]  # replayed
+    assert again.device["gpu_launches"] == first.device["gpu_launches"]
     assert first.count == again.count == ref.count
     assert _layers(again) == _layers(ref)
 
@@ -159,7 +160,7 @@ def test_autotune_picks_a_grid_point_and_caches_it(tctx, qp, tmp_path):
     out = tctx.autotune(n=12, repeats=1, cache=cache)
     assert not out["cached"] and out["device_ms"] > 0
     t = out["tuning"]
-    assert t["scatter_kind"] in (0, 1, 2, 3, 4) and t["parents_per_lane"] in (2, 4) and t["merge_kind"] in (0, 1)
+    assert t["scatter_kind"] in (0, 1, 2, 4) and t["parents_per_lane"] in (2, 4) and t["merge_kind"] in (0, 1)
     assert t["scatter_block"] in (128, 256, 512) and t["batch_lanes"] == 1 and t["slice_rows"] in (1, 2)
     assert t["merge_auto"] in (qp.MERGE_PARTITION, qp.MERGE_HASH)
     assert tctx.tuning["scatter_kind"] == t["scatter_kind"]
