@@ -295,6 +295,10 @@ def run_ours(args):
         opts["granularity"] = pkg.GRAIN_SITE
     if args.tail_row is not None:
         opts["tail_row"] = args.tail_row
+    if args.key_bits:
+        opts["key_bits"] = args.key_bits
+    if args.merge:
+        opts["merge"] = {"hash": pkg.MERGE_HASH, "partition": pkg.MERGE_PARTITION}[args.merge]
     merged = (merged_entries(pkg, args.n, device, opts)
               if args.grain == "row" and not args.no_merged_run else None)
     ctx = pkg.Context(device)
@@ -600,6 +604,10 @@ def main():
     ap.add_argument("--n", type=int, default=18)
     ap.add_argument("--grain", choices=["row", "site"], default="row")
     ap.add_argument("--slice-depth", type=int, default=0)
+    ap.add_argument("--key-bits", type=int, choices=[0, 64, 128], default=0,
+                    help="boundary key width (0: the library's choice, u64 up to N=21)")
+    ap.add_argument("--merge", choices=["", "hash", "partition"], default="",
+                    help="merge strategy (default: the library's choice)")
     ap.add_argument("--tail-row", type=int, default=None,
                     help="first row run by the slice-tail kernel (default: library auto; >= n disables it)")
     ap.add_argument("--cpu-rows", type=int, default=9)
