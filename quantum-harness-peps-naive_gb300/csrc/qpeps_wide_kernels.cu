@@ -297,7 +297,9 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
       u32 slot = 0;
       if (i < bcnt) {
         const u128 key = buf[l].key;
-        slot = (u32)(key_hash<u128>(key) >> (64 - kLogH));
+        // The partition index takes the hash's top bits; the slot re-mixes
+        // the whole hash so keys of one partition spread over the table.
+        slot = (u32)(fib_hash_b(key_hash<u128>(key)) >> (64 - kLogH));
         for (int probe = 0; probe < H; ++probe) {
           const u128 cur = wscas(&s_key[slot], kWEmpty, key);
           if (cur == kWEmpty || cur == key) {
