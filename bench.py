@@ -595,6 +595,46 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_explicit(args):
+    """The explicit-C site frontier (contract_explicit_c_frontier,
+    src/lib.rs:961-967) at one N and order, through the partitioned merge
+    (default) and through the global table; one JSON line, wall time of the
+    default path as the value."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = importlib.import_module(PACKAGE)
+    if not pkg.LIBRARY_PATH.exists():
+        pkg.build()
+    order = {"row": pkg.ORDER_ROW_MAJOR, "diamond": pkg.ORDER_TOP_LEFT_DIAMOND}[args.explicit_order]
+    fields = ("count", "complete", "peak_states", "peak_open_bonds", "tensor_entries_examined",
+              "tensor_entries_accepted", "contracted_sites")
+    arms = {}
+    for name, merge in (("partition", pkg.MERGE_PARTITION), ("hash", pkg.MERGE_HASH)):
+        ctx = pkg.Context(0)
+        ctx.set_tuning(merge_auto=merge)
+        for _ in range(args.warmup):
+            ctx.explicit_frontier(args.explicit, order)
+        walls, dev = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = ctx.explicit_frontier(args.explicit, order)
+            walls.append(time.perf_counter() - t0)
+            dev.append(r["device_ms"])
+        ctx.close()
+        arms[name] = {"wall_ms": statistics.median(walls) * 1e3, "device_ms": statistics.median(dev),
+                      "gpu_launches": r["gpu_launches"], **{k: r[k] for k in fields}}
+    same = all(arms["partition"][k] == arms["hash"][k] for k in fields)
+    line = {"metric": "explicit-C site frontier wall time", "value": arms["partition"]["wall_ms"], "unit": "ms",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "u128 keys + u32 residues", "data": "none (the count of the N x N board)",
+            "config": {"workload": "explicit-C site frontier, N=%d, %s order" % (args.explicit, args.explicit_order)},
+            "count": str(arms["partition"]["count"]), "partition_equals_hash": same, "arms": arms}
+    print(json.dumps(line, default=str), flush=True)
+    if not same:
+        sys.exit(1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -627,6 +667,9 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="contract eagerly every step (default: the first warm-up step captures the row steps "
                          "as a CUDA graph and later steps replay it)")
+    ap.add_argument("--explicit", type=int, default=0,
+                    help="time the explicit-C site frontier at this N instead of the Q(N) step")
+    ap.add_argument("--explicit-order", choices=["row", "diamond"], default="diamond")
     ap.add_argument("--serve", action="store_true", help="run the serving stream instead of the Q(N) step")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-requests-inline", type=int, default=1000,
@@ -644,6 +687,8 @@ def main():
     args = ap.parse_args()
     if args.serve:
         run_serve(args)
+    elif args.explicit:
+        run_explicit(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -1241,6 +1241,73 @@ struct ExplicitRun {
   u128 examined = 0, accepted = 0;
 };
 
+// One explicit-C frontier step through the 128-bit partitions, in place:
+// count the (entry, matching transition) pairs, size the partitions from
+// that count, scatter, merge. Returns the count; the merged boundary's
+// scalars are left in ctx.h_sc. An overflowing partition makes the merge
+// write nothing, so the step is retried with smaller partitions.
+static u64 explicit_partition_step(Ctx& ctx, const Plan& p, DevFrontier& f, const FrontierStepDev& st,
+                                   ExplicitRun& out) {
+  float ms = 0;
+  cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
+  cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+  cuda_check(launch_frontier_count(view_of(p, ctx.front[0], f.cap), f.count, st, ctx.sms, ctx.d_sc, ctx.stream),
+             "frontier count kernel");
+  cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+  out.launches += f.count ? 1 : 0;
+  sync_scalars(ctx);
+  cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
+  out.device_ms += ms;
+  const u64 terms = ctx.h_sc->terms;
+  if (terms == 0) return 0;  // the scalars read back say: no entries, zero weight
+  const u32 pcap = wide_key_partition_capacity();
+  double mean = ctx.partition_fill * pcap;
+  for (int attempt = 0;; ++attempt) {
+    const u64 parts64 = std::max<u64>(1, (u64)((double)terms / mean) + 1);
+    if (parts64 > 0xffffffffull) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier needs too many partitions");
+    const u32 parts = (u32)parts64;
+    const u32 cstride = (parts <= ctx.tune.spread_cursors_below) ? 8u : 1u;
+    const size_t region_bytes = (size_t)parts * pcap * cand_bytes(p);
+    const size_t table_bytes = region_bytes + ((size_t)parts * 4 * cstride + 255) / 256 * 256;
+    if (ctx.table.bytes < table_bytes) buf_release(ctx, ctx.table);
+    if (!ensure_front(ctx, p, f, std::max<u64>(f.count, terms), ctx.table.ptr ? 0 : table_bytes))
+      fail(QPEPS_ERR_CAPACITY, "device budget exceeded by the explicit-C frontier");
+    buf_reserve(ctx, ctx.table, table_bytes, p.budget, "explicit-C frontier partitions");
+    const FrontierView view = view_of(p, ctx.front[0], f.cap);
+    void* regions = ctx.table.ptr;
+    u32* cursors = reinterpret_cast<u32*>(static_cast<char*>(ctx.table.ptr) + region_bytes);
+    PartitionCfg pc{};
+    pc.residues = p.R;
+    pc.sms = ctx.sms;
+    pc.parts = parts;
+    pc.cap = pcap;
+    pc.merge_blocks_per_sm = 2;
+    pc.cursor_stride = cstride;
+    pc.key_bits = 128;
+    cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
+    cuda_check(cudaMemsetAsync(cursors, 0, (size_t)parts * 4 * cstride, ctx.stream), "clear partition cursors");
+    cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+    cuda_check(launch_frontier_partition_scatter(pc, view, f.count, st, regions, cursors, ctx.d_sc, ctx.stream),
+               "frontier scatter kernel");
+    cuda_check(launch_wide_partition_merge(pc, regions, cursors, view, 0, true, ctx.d_sc, ctx.stream),
+               "frontier merge kernel");
+    cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+    out.launches += 2;
+    sync_scalars(ctx);
+    cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
+    out.device_ms += ms;
+    if (ctx.h_sc->error & kErrBounds)
+      fail(QPEPS_ERR_CUDA, "explicit-C frontier: a kernel's bounds check failed (access skipped)");
+    if (ctx.h_sc->error & kErrOverflow) {
+      if (attempt >= 4) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier: partition overflow persists");
+      mean *= 0.6;
+      continue;
+    }
+    if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier: device capacity error");
+    return terms;
+  }
+}
+
 static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_limit, ExplicitRun& out) {
   const auto t0 = std::chrono::steady_clock::now();
   if (n > 21) fail(QPEPS_ERR_RANGE, "explicit-C frontier key supports N <= 21");
@@ -1365,6 +1432,26 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
       ++st.n_trans;
     }
     out.examined += (u128)f.count * 17;
+    // The partitioned merge unless the tuning asks for the global table, or
+    // a key could set all 128 bits (the partition tables' empty marker).
+    if (ctx.tune.merge_auto != QPEPS_MERGE_HASH && next.size() < 128) {
+      const u64 terms = explicit_partition_step(ctx, p, f, st, out);
+      out.accepted += terms;
+      const u64 merged = ctx.h_sc->out_count;
+      if (merged > support_limit) {
+        out.peak_states = std::max<u64>(out.peak_states, support_limit + 1);
+        out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next.size());
+        out.contracted_sites = step;
+        out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return;
+      }
+      f.count = merged;
+      for (int r = 0; r < p.R; ++r) weight_res[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
+      open.swap(next);
+      out.peak_states = std::max<u64>(out.peak_states, merged);
+      out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, open.size());
+      continue;
+    }
     // Every incoming leg of a site is a bond of an earlier site or a board
     // edge in both orders, so at most two C entries match a key.
     const u64 need = std::max<u64>(f.count * 2, 1);

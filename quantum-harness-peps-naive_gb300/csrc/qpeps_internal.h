@@ -138,6 +138,15 @@ cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const Frontier
 cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                         const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
                                         cudaStream_t stream);
+// Explicit-C frontier step through the same 128-bit partitions: the number of
+// (boundary entry, matching transition) pairs into `scalars->terms`, and
+// every such pair as one candidate (merged by launch_wide_partition_merge
+// with n = 0). Keys must not set all 128 bits (at most 127 open bonds).
+cudaError_t launch_frontier_count(const FrontierView& in, uint64_t n_in, const FrontierStepDev& step, int sms,
+                                  StepScalars* scalars, cudaStream_t stream);
+cudaError_t launch_frontier_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in,
+                                              const FrontierStepDev& step, void* regions, uint32_t* cursors,
+                                              StepScalars* scalars, cudaStream_t stream);
 // Candidate slots per partition for a merge shape (PartitionCfg::wide).
 uint32_t partition_capacity(uint32_t wide = 0);
 // Whether the wide merge shape is available for a residue count.

@@ -386,6 +386,58 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
 }
 
+// ---------------------------------------------------------------------------
+// Explicit-C site frontier through the same partitions. A step's transitions
+// (bond runs that move, and per matching C entry the required and added bond
+// values) come as a kernel parameter; every (boundary entry, matching
+// transition) pair is one candidate with the entry's residues. At most two C
+// entries match a key, so a thread writes its entry's candidates directly.
+
+__device__ __forceinline__ u128 wshift(u128 v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) frontier_count_kernel(const u128* __restrict__ keys, u64 n_in,
+                                                              const __grid_constant__ FrontierStepDev st,
+                                                              StepScalars* __restrict__ sc) {
+  unsigned long long acc = 0;
+  for (u64 i = (u64)blockIdx.x * BLOCK + threadIdx.x; i < n_in; i += (u64)gridDim.x * BLOCK) {
+    const u128 key = keys[i];
+    for (u32 t = 0; t < st.n_trans; ++t) acc += (key & st.req_mask[t]) == st.req_value[t];
+  }
+  const unsigned long long t = wblock_sum<BLOCK>(acc);
+  if (threadIdx.x == 0 && t) atomicAdd(&sc->terms, t);
+}
+
+template <int R, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) frontier_scatter_kernel(const u128* __restrict__ keys,
+                                                                const u32* __restrict__ res, u64 res_stride,
+                                                                u64 n_in, const __grid_constant__ FrontierStepDev st,
+                                                                WCand<R>* __restrict__ regions,
+                                                                u32* __restrict__ cursors, u32 cstride, u32 parts,
+                                                                u32 cap, StepScalars* __restrict__ sc) {
+  const u64 policy = wl2_keep_policy();
+  bool overflow = false;
+  for (u64 i = (u64)blockIdx.x * BLOCK + threadIdx.x; i < n_in; i += (u64)gridDim.x * BLOCK) {
+    const u128 key = wload_key(keys + i);
+    u128 moved = 0;
+    for (u32 r = 0; r < st.n_runs; ++r) moved |= wshift(key & st.run_mask[r], st.run_shift[r]);
+    WCand<R> c;
+#pragma unroll
+    for (int r = 0; r < R; ++r) c.res[r] = __ldcs(res + r * res_stride + i);
+    for (u32 t = 0; t < st.n_trans; ++t) {
+      if ((key & st.req_mask[t]) != st.req_value[t]) continue;
+      c.key = moved | st.added[t];
+      const u32 part = wpartition_of(c.key, parts);
+      const u32 pos = atomicAdd(&cursors[(u64)part * cstride], 1u);
+      if (pos < cap)
+        wstore<R>(regions + (u64)part * cap + pos, c, policy);
+      else
+        overflow = true;
+    }
+  }
+  if (overflow) atomicOr(&sc->error, kErrOverflow);
+}
+
 constexpr int kWScatterBlock = 256;
 
 template <int R>
@@ -441,6 +493,45 @@ cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regi
     case 4: return wide_merge<4>(pc, regions, cursors, out, n, write_out, sc, stream);
   }
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_frontier_count(const FrontierView& in, uint64_t n_in, const FrontierStepDev& step, int sms,
+                                  StepScalars* sc, cudaStream_t stream) {
+  if (n_in == 0) return cudaSuccess;
+  if (n_in > in.cap || step.n_trans > (uint32_t)kFrontierMaxTrans) return cudaErrorInvalidValue;
+  const u64 want = (n_in + kWScatterBlock - 1) / kWScatterBlock;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(want, (u64)sms * 8));
+  frontier_count_kernel<kWScatterBlock><<<grid, kWScatterBlock, 0, stream>>>(reinterpret_cast<const u128*>(in.keys),
+                                                                             n_in, step, sc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frontier_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in,
+                                              const FrontierStepDev& step, void* regions, uint32_t* cursors,
+                                              StepScalars* sc, cudaStream_t stream) {
+  if (n_in == 0) return cudaSuccess;
+  if (n_in > in.cap || pc.parts == 0 || pc.cap != (u32)kWCap || step.n_trans > (uint32_t)kFrontierMaxTrans ||
+      step.n_runs > (uint32_t)kFrontierMaxRuns)
+    return cudaErrorInvalidValue;
+  const u64 want = (n_in + kWScatterBlock - 1) / kWScatterBlock;
+  const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(want, (u64)pc.sms * 8));
+  const u128* keys = reinterpret_cast<const u128*>(in.keys);
+  const u32 cs = pc.cursor_stride ? pc.cursor_stride : 1;
+  switch (pc.residues) {
+#define QPEPS_FRONTIER_SCATTER(R)                                                                            \
+  case R:                                                                                                   \
+    frontier_scatter_kernel<R, kWScatterBlock><<<grid, kWScatterBlock, 0, stream>>>(                         \
+        keys, in.res, in.cap, n_in, step, reinterpret_cast<WCand<R>*>(regions), cursors, cs, pc.parts, pc.cap, sc); \
+    break;
+    QPEPS_FRONTIER_SCATTER(1)
+    QPEPS_FRONTIER_SCATTER(2)
+    QPEPS_FRONTIER_SCATTER(3)
+    QPEPS_FRONTIER_SCATTER(4)
+#undef QPEPS_FRONTIER_SCATTER
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 static_assert(sizeof(WCand<1>) == 32 && sizeof(WCand<4>) == 32, "32-byte wide candidates");

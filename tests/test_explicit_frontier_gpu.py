@@ -60,3 +60,40 @@ def test_range_and_argument_errors(ctx, qp):
     with pytest.raises(qp.ContractionError) as e:
         ctx.explicit_frontier(5, 0, 0)
     assert e.value.code == qp.QPEPS_ERR_INVALID and "support limit must be positive" in e.value.message
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_partitioned_merge_equals_global_table(qp, order):
+    """The explicit-C frontier through the 128-bit partitions (the default)
+    and through the global table (merge_auto = MERGE_HASH) agree on every
+    field, complete and stopped at a support limit; the partitioned steps
+    launch a count, a scatter and a merge kernel."""
+    part, table = qp.Context(0), qp.Context(0)
+    try:
+        table.set_tuning(merge_auto=qp.MERGE_HASH)
+        for n in range(1, 13):
+            a, b = part.explicit_frontier(n, order), table.explicit_frontier(n, order)
+            assert {k: a[k] for k in FIELDS} == {k: b[k] for k in FIELDS}, n
+            assert a["gpu_launches"] > b["gpu_launches"]
+        for limit in (50, 3000, 200_000):
+            a, b = part.explicit_frontier(11, order, limit), table.explicit_frontier(11, order, limit)
+            assert {k: a[k] for k in FIELDS} == {k: b[k] for k in FIELDS}, limit
+    finally:
+        part.close()
+        table.close()
+
+
+def test_partition_overflow_retries_exactly(qp, golden):
+    """At fill 0.95 partitions of 1024 slots overflow on large steps; the
+    merge then writes nothing and the step is retried with smaller
+    partitions, so the published counters still hold."""
+    c = qp.Context(0)
+    try:
+        c.set_tuning(partition_fill=0.95)
+        for name, order in ORDERS.items():
+            want = golden["explicit_frontier"][name]["12"]
+            r = c.explicit_frontier(12, order, want["support_limit"])
+            assert r["count"] == want["count"] and r["peak_states"] == want["peak_support"]
+            assert r["tensor_entries_accepted"] == want["tensor_entries_accepted"]
+    finally:
+        c.close()
