@@ -468,8 +468,11 @@ struct HostChunk {
   std::vector<uint32_t> res;  // R planes of `count`
 };
 
+constexpr u64 kTermsUnknown = ~0ull;
+
 struct StepOut {
   u64 in = 0, terms = 0, out = 0;
+  u64 next_terms = kTermsUnknown;  // the output boundary's successor terms at the next row, if the merge counted them
   u64 exact_sum = 0;  // w64: exact total weight of the output boundary
   u64 weight[kMaxResidues] = {0, 0, 0, 0};
   u64 final_sum[kMaxResidues] = {0, 0, 0, 0};
@@ -586,12 +589,14 @@ static UnitClassPlan unit_class_plan(unsigned n, unsigned filled, u64 terms, u32
 }
 
 // One merge step (a row in row grain, a site in site grain), in place.
+// `known_terms`: the step's successor count when the previous row's merge
+// counted it for exactly this boundary (no counting pass then).
 static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site, unsigned site_idx, bool final_step,
-                             RunStats& rs, unsigned row, StepOut* so_out) {
+                             RunStats& rs, unsigned row, StepOut* so_out, u64 known_terms = kTermsUnknown) {
   StepOut so;
   const u64 n_in = f.count;
   so.in = n_in;
-  so.terms = count_terms(ctx, p, f, site, site_idx, rs);
+  so.terms = (known_terms != kTermsUnknown && !site) ? known_terms : count_terms(ctx, p, f, site, site_idx, rs);
   if (so.terms == 0) {
     f.count = 0;
     *so_out = so;
@@ -748,6 +753,7 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
       ms_a += ms_plan;
     }
     so.out = ctx.h_sc->out_count;
+    if (!final_step && ctx.h_sc->next_terms_ok) so.next_terms = ctx.h_sc->next_terms;
     so.exact_sum = ctx.h_sc->weight_sum[0];
     for (int r = 0; r < p.Rc; ++r) {
       // Exact weights: plane 0 carries the exact sums.
@@ -976,6 +982,7 @@ static void run_chunks(Ctx& ctx, const Plan& p, std::vector<HostChunk> pending, 
     rs.peak_states = std::max<u64>(rs.peak_states, f.count);
     unsigned site0 = hc.site;
     bool counted = hc.row_counted;
+    u64 known_terms = kTermsUnknown;  // successor count of the live boundary, when a merge counted it
     const unsigned stop = hc.no_tail ? p.n : std::max(p.tail_row, hc.row);
     for (unsigned row = hc.row; row < stop; ++row) {
       const auto t0 = std::chrono::steady_clock::now();
@@ -1014,8 +1021,11 @@ static void run_chunks(Ctx& ctx, const Plan& p, std::vector<HostChunk> pending, 
           const u128 bound = f.weight_bound * (u128)(p.n - row);
           if (bound >> 63) fail(QPEPS_ERR_OVERFLOW, row_msg("exact 64-bit weights are not certified at row", row + 1));
         }
-        while (merge_step(ctx, p, f, false, 0, last_row, rs, row, &so) == StepStatus::NeedSplit)
+        while (merge_step(ctx, p, f, false, 0, last_row, rs, row, &so, known_terms) == StepStatus::NeedSplit) {
           split_to_host(ctx, p, f, row, 0, false, hc.no_tail, pending);
+          known_terms = kTermsUnknown;  // the boundary was halved
+        }
+        known_terms = so.next_terms;
         if (p.w64) f.weight_bound = so.exact_sum;
         acc.input_states += so.in;
         acc.candidates += (u128)so.in * p.n;

@@ -34,11 +34,11 @@ struct StepScalars {
   unsigned long long final_sum[4];   // sum of residues of entries with all columns set
   unsigned long long final_states;   // entries with all columns set
   unsigned int error;                // ErrorBits
-  unsigned int pad0;
+  unsigned int next_terms_ok;        // 1: the merge counted next_terms (fixed-layout row merges)
   unsigned long long sitewise_examined;  // row count: C entries the reference's per-parent sitewise
                                          // row kernel matches over the input (sitewise_entries())
   unsigned long long plan_units;         // class-grouped partitions: units of the step's plan (graph replay)
-  unsigned int pad[2];
+  unsigned long long next_terms;         // successor terms of the written boundary at the next row
 };
 
 struct LaunchCfg {

@@ -638,6 +638,17 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   }
 }
 
+// Free columns of a fixed-layout boundary key at the next row: the successor
+// terms it will generate there (what row_count_kernel sums).
+__device__ __forceinline__ unsigned long long next_terms_of(const FixedLayout& L, u64 key) {
+  const State st = L.unpack(key);
+  return (unsigned long long)__popcll(~(st.cols | st.dr | st.dl) & L.mask);
+}
+template <typename Layout>
+__device__ __forceinline__ unsigned long long next_terms_of(const Layout&, u64) {
+  return 0ull;
+}
+
 // Listed variant of the merge, in three phases per partition:
 //   1. every candidate claims or finds its key's slot with one shared-memory
 //      compare-and-swap; a key's first claimant appends the slot to a list
@@ -708,6 +719,10 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
     for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK) s_slot_fin[i] = 0ull;
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
   unsigned long long wsum[R], fsum[R], fstates = 0;
+  // The written boundary's successor terms at the next row (the next row
+  // step's count, so that it needs no counting pass of its own).
+  unsigned long long nterms = 0;
+  constexpr bool kCountNext = !Layout::kSlotted;
   bool bad = false;  // an output index beyond the boundary buffer (skipped)
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
@@ -835,6 +850,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
           const bool wr = write_out && idx < out_stride;
           bad |= write_out && !wr;
           if (wr) keys_out[idx] = key;
+          if constexpr (kCountNext) nterms += next_terms_of(L, key);
           const u64 folded = kFold ? s_acc[slot] : 0ull;
           if constexpr (kAcc == 2) {
             if (wr) {
@@ -867,6 +883,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
       const bool wr = write_out && idx < out_stride;
       bad |= write_out && !wr;
       if (wr) keys_out[idx] = key;
+      if constexpr (kCountNext) nterms += next_terms_of(L, key);
       const u64 folded = kFold ? s_acc[slot] : 0ull;
       if constexpr (kAcc == 2) {
         if (wr) {
@@ -899,6 +916,13 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   }
   const unsigned long long t = pblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+  if constexpr (kCountNext) {
+    if (write_out) {
+      const unsigned long long nt = pblock_sum<BLOCK>(nterms);
+      if (threadIdx.x == 0 && nt) atomicAdd(&sc->next_terms, nt);
+      if (blockIdx.x == 0 && threadIdx.x == 0) sc->next_terms_ok = 1u;
+    }
+  }
   if constexpr (Layout::kSlotted) {
     __syncthreads();
     for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK)

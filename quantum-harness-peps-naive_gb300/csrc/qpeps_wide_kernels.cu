@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
   const u64 mask = (n >= 64) ? ~0ull : ((1ull << n) - 1);
   unsigned long long wsum[R], fsum[R], fstates = 0;
+  unsigned long long nterms = 0;  // the written boundary's successor terms at the next row (n > 0)
   bool bad = false;
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
@@ -362,6 +363,10 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
         kv.y = (u64)(key >> 64);
         reinterpret_cast<ulonglong2*>(keys_out)[idx] = kv;
       }
+      if (n) {
+        const State st = unpack<u128>(key, n, mask);
+        nterms += __popcll(~(st.cols | st.dr | st.dl) & mask);
+      }
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const u32 v = reduce_sum(s_acc[r * H + slot], r);
@@ -384,6 +389,11 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
   }
   const unsigned long long t = wblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+  if (write_out && n) {
+    const unsigned long long nt = wblock_sum<BLOCK>(nterms);
+    if (threadIdx.x == 0 && nt) atomicAdd(&sc->next_terms, nt);
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->next_terms_ok = 1u;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -358,3 +358,19 @@ def test_slice_tail_at_n17(ctx, oracle):
     assert g.count == oracle.known_count(17)
     merged = ctx.contract_rows(17)
     assert merged.device["tail_row"] == 17 and merged.count == g.count
+
+
+@pytest.mark.parametrize("key_bits", [64, 128])
+@pytest.mark.parametrize("n", [9, 13])
+def test_merge_counts_the_next_rows_terms(ctx, oracle, n, key_bits):
+    """The partitioned merge counts the successor terms of the boundary it
+    writes, so after the first device row an eager contraction runs no
+    counting kernel: one count, then a scatter and a merge per row and batch,
+    with every row's terms still equal to the oracle's."""
+    g = ctx.contract_rows(n, key_bits=key_bits, use_graph=0)
+    o = oracle.contract(n, backend=O.SORT_REDUCE)
+    assert g.count == o["count"]
+    assert _gpu_layers(g) == _oracle_layers(o)
+    d = g.device
+    device_rows = n - d["slice_depth"]
+    assert d["gpu_launches"] == d["batches"] * (1 + 2 * device_rows)
