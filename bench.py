@@ -614,11 +614,11 @@ def run_explicit(args):
         ctx = pkg.Context(0)
         ctx.set_tuning(merge_auto=merge)
         for _ in range(args.warmup):
-            ctx.explicit_frontier(args.explicit, order)
+            ctx.explicit_frontier(args.explicit, order, args.explicit_limit)
         walls, dev = [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            r = ctx.explicit_frontier(args.explicit, order)
+            r = ctx.explicit_frontier(args.explicit, order, args.explicit_limit)
             walls.append(time.perf_counter() - t0)
             dev.append(r["device_ms"])
         ctx.close()
@@ -628,7 +628,8 @@ def run_explicit(args):
     line = {"metric": "explicit-C site frontier wall time", "value": arms["partition"]["wall_ms"], "unit": "ms",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
             "dtype": "u128 keys + u32 residues", "data": "none (the count of the N x N board)",
-            "config": {"workload": "explicit-C site frontier, N=%d, %s order" % (args.explicit, args.explicit_order)},
+            "config": {"workload": "explicit-C site frontier, N=%d, %s order" % (args.explicit, args.explicit_order),
+                       "support_limit": args.explicit_limit},
             "count": str(arms["partition"]["count"]), "partition_equals_hash": same, "arms": arms}
     print(json.dumps(line, default=str), flush=True)
     if not same:
@@ -670,6 +671,7 @@ def main():
     ap.add_argument("--explicit", type=int, default=0,
                     help="time the explicit-C site frontier at this N instead of the Q(N) step")
     ap.add_argument("--explicit-order", choices=["row", "diamond"], default="diamond")
+    ap.add_argument("--explicit-limit", type=int, default=5_000_000, help="support limit of the explicit-C frontier")
     ap.add_argument("--serve", action="store_true", help="run the serving stream instead of the Q(N) step")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-requests-inline", type=int, default=1000,
