@@ -2682,6 +2682,9 @@ static double autotune(Ctx& c, unsigned n, unsigned repeats, Ctx::Tune* best) {
       {{QPEPS_MERGE_PARTITION, QPEPS_MERGE_HASH}, [](Ctx::Tune& t, double v) { t.merge_auto = (uint32_t)v; }},
       {{5, 3, 8}, [](Ctx::Tune& t, double v) { t.slice_margin = v; }},
       {{1, 2}, [](Ctx::Tune& t, double v) { t.slice_rows = (uint32_t)v; }},
+      // Concurrent batch lanes of the graph replay (used with the window and
+      // direct scatters only; other scatter kinds replay on one lane).
+      {{1, 2}, [](Ctx::Tune& t, double v) { t.batch_lanes = (uint32_t)v; }},
   };
   try {
     best_ms = measure(cur, 1e300);

@@ -470,6 +470,17 @@ __global__ void __launch_bounds__(BLOCK, (kPPL <= 2 ? 4 : 3)) partition_scatter_
 
 constexpr u64 kEmpty = kEmptyKey;
 
+// Free columns of a fixed-layout boundary key at the next row: the successor
+// terms it will generate there (what row_count_kernel sums).
+__device__ __forceinline__ unsigned long long next_terms_of(const FixedLayout& L, u64 key) {
+  const State st = L.unpack(key);
+  return (unsigned long long)__popcll(~(st.cols | st.dr | st.dl) & L.mask);
+}
+template <typename Layout>
+__device__ __forceinline__ unsigned long long next_terms_of(const Layout&, u64) {
+  return 0ull;
+}
+
 template <int R, int BLOCK, int H, int CAP, typename Layout>
 __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* __restrict__ regions,
                                                                 const u32* __restrict__ cursors, u32 cstride,
@@ -498,6 +509,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   // host's retry with smaller partitions.
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
   unsigned long long wsum[R], fsum[R], fstates = 0;
+  unsigned long long nterms = 0;  // the written boundary's successor terms at the next row
   bool bad = false;  // an output index beyond the boundary buffer (skipped)
 #pragma unroll
   for (int r = 0; r < R; ++r) wsum[r] = fsum[r] = 0;
@@ -607,6 +619,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
         const bool wr = write_out && idx < out_stride;
         bad |= write_out && !wr;
         if (wr) keys_out[idx] = key;
+        if constexpr (!Layout::kSlotted) nterms += next_terms_of(L, key);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const u32 v = reduce_sum(s_acc[r * H + slot], r);
@@ -631,22 +644,18 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   }
   const unsigned long long t = pblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
+  if constexpr (!Layout::kSlotted) {
+    if (write_out) {
+      const unsigned long long nt = pblock_sum<BLOCK>(nterms);
+      if (threadIdx.x == 0 && nt) atomicAdd(&sc->next_terms, nt);
+      if (blockIdx.x == 0 && threadIdx.x == 0) sc->next_terms_ok = 1u;
+    }
+  }
   if constexpr (Layout::kSlotted) {
     __syncthreads();
     for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK)
       if (s_slot_fin[i]) atomicAdd(&L.slot_final[(i / R) * 4 + (i % R)], s_slot_fin[i]);
   }
-}
-
-// Free columns of a fixed-layout boundary key at the next row: the successor
-// terms it will generate there (what row_count_kernel sums).
-__device__ __forceinline__ unsigned long long next_terms_of(const FixedLayout& L, u64 key) {
-  const State st = L.unpack(key);
-  return (unsigned long long)__popcll(~(st.cols | st.dr | st.dl) & L.mask);
-}
-template <typename Layout>
-__device__ __forceinline__ unsigned long long next_terms_of(const Layout&, u64) {
-  return 0ull;
 }
 
 // Listed variant of the merge, in three phases per partition:

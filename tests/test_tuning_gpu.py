@@ -161,7 +161,7 @@ def test_autotune_picks_a_grid_point_and_caches_it(tctx, qp, tmp_path):
     assert not out["cached"] and out["device_ms"] > 0
     t = out["tuning"]
     assert t["scatter_kind"] in (0, 1, 2, 4) and t["parents_per_lane"] in (2, 4) and t["merge_kind"] in (0, 1)
-    assert t["scatter_block"] in (128, 256, 512) and t["batch_lanes"] == 1 and t["slice_rows"] in (1, 2)
+    assert t["scatter_block"] in (128, 256, 512) and t["batch_lanes"] in (1, 2) and t["slice_rows"] in (1, 2)
     assert t["merge_auto"] in (qp.MERGE_PARTITION, qp.MERGE_HASH)
     assert tctx.tuning["scatter_kind"] == t["scatter_kind"]
     entries = json.loads(cache.read_text())
