@@ -88,3 +88,20 @@ def test_no_host_fallback_without_a_device(qp):
     assert e.value.code == qp.QPEPS_ERR_CUDA
     with pytest.raises(qp.ContractionError):
         qp.contract_rows(8)
+
+
+def test_shipped_tuning_cache_matches_this_library(qp):
+    """Every entry of the GB300 tuning cache is keyed by this library's
+    version and names only fields of qpeps_tuning, within their ranges."""
+    import json
+
+    entries = json.loads((qp.LIBRARY_PATH.parent / "tuning_gb300.json").read_text())
+    fields = {name for name, _ in qp.Tuning._fields_} - {"struct_size", "reserved"}
+    assert entries
+    for key, e in entries.items():
+        device, ver, probe = key.split("|")
+        assert device == "NVIDIA GB300" and ver == qp.version() and probe.startswith("n=")
+        t = e["tuning"]
+        assert set(t) <= fields and e["device_ms"] > 0
+        assert 0.3 <= t["partition_fill"] <= 0.95 and 1 <= t["batch_lanes"] <= 8 and 1.0 <= t["slice_margin"] <= 64
+        assert t["scatter_kind"] in (0, 1, 2, 4)  # the class-grouped scatter is never cached
