@@ -636,6 +636,36 @@ def run_explicit(args):
         sys.exit(1)
 
 
+def run_probe(args):
+    """The partition scatter's memory pattern alone (qpeps_probe_append):
+    random 16-byte appends with one cursor atomic each, the stores without the
+    atomics, the atomics without the stores, and coalesced stores, at the
+    scatter's partition sizing; one JSON line with each mode's best rate."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = importlib.import_module(PACKAGE)
+    if not pkg.LIBRARY_PATH.exists():
+        pkg.build()
+    ctx = pkg.Context(0)
+    cases = []
+    for cand in args.probe_candidates:
+        parts = max(1, int(cand / (args.probe_fill * 2048)) + 1)
+        row = {"candidates": cand, "parts": parts, "fill": args.probe_fill}
+        for name, mode in (("append", pkg.PROBE_APPEND), ("store_only", pkg.PROBE_STORE),
+                           ("atomic_only", pkg.PROBE_ATOMIC), ("stream", pkg.PROBE_STREAM)):
+            ms = ctx.probe_append(mode, cand, parts, repeats=args.steps)
+            row[name] = {"ms": ms, "records_per_s": cand / (ms * 1e-3), "gb_per_s": cand * 16 / (ms * 1e-3) / 1e9}
+        cases.append(row)
+    ctx.close()
+    line = {"metric": "partition scatter pattern rate (16-byte records into hash partitions)", "unit": "records/s",
+            "value": cases[0]["append"]["records_per_s"], "n_gpus": 1, "steps": args.steps, "warmup": 1,
+            "higher_is_better": True, "data": "synthetic (pseudo-random keys)",
+            "config": {"workload": "random appends into partitions of 2048 16-byte slots", "fill": args.probe_fill},
+            "cases": cases}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -668,6 +698,10 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="contract eagerly every step (default: the first warm-up step captures the row steps "
                          "as a CUDA graph and later steps replay it)")
+    ap.add_argument("--probe", action="store_true",
+                    help="time the partition scatter's memory pattern alone instead of the Q(N) step")
+    ap.add_argument("--probe-candidates", type=int, nargs="+", default=[64 << 20, 512 << 20])
+    ap.add_argument("--probe-fill", type=float, default=0.75)
     ap.add_argument("--explicit", type=int, default=0,
                     help="time the explicit-C site frontier at this N instead of the Q(N) step")
     ap.add_argument("--explicit-order", choices=["row", "diamond"], default="diamond")
@@ -689,6 +723,8 @@ def main():
     args = ap.parse_args()
     if args.serve:
         run_serve(args)
+    elif args.probe:
+        run_probe(args)
     elif args.explicit:
         run_explicit(args)
     elif args.impl == "reference":

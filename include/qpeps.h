@@ -274,6 +274,21 @@ int qpeps_autotune(void* ctx, uint32_t n, uint32_t repeats, qpeps_tuning* best, 
 /* Name of the context's CUDA device (for keying tuning caches). */
 int qpeps_ctx_device_name(void* ctx, char* out, size_t len);
 
+/* Device rate of the partition scatter's memory pattern, as a ceiling to
+ * judge the scatter against (no reference counterpart): `candidates`
+ * pseudo-random 16-byte records into `parts` partitions of 2048 slots, by
+ * `mode`: QPEPS_PROBE_APPEND (one cursor atomic takes each record's slot, as
+ * in the scatter), QPEPS_PROBE_STORE (stores to random slots, no atomic),
+ * QPEPS_PROBE_ATOMIC (the atomics, no store), QPEPS_PROBE_STREAM (coalesced
+ * stores). `best_ms`: the best CUDA-event time of `repeats` launches after
+ * one untimed launch. Needs parts * 32 KiB of free device memory. */
+#define QPEPS_PROBE_APPEND 0
+#define QPEPS_PROBE_STORE 1
+#define QPEPS_PROBE_ATOMIC 2
+#define QPEPS_PROBE_STREAM 3
+int qpeps_probe_append(void* ctx, uint32_t mode, uint64_t candidates, uint32_t parts, uint32_t repeats,
+                       double* best_ms, char* err, size_t err_len);
+
 /* ---- Serving: continuous batching of counting requests -------------------
  * No single reference counterpart: each request is the prefix contraction of
  * qpeps_count (contract_rows, src/lib.rs:758, from a placed prefix). A server

@@ -161,6 +161,10 @@ class ServeStats(ctypes.Structure):
                           "coalesced")]
 
 
+PROBE_APPEND = 0
+PROBE_STORE = 1
+PROBE_ATOMIC = 2
+PROBE_STREAM = 3
 ORDER_ROW_MAJOR = 0
 ORDER_TOP_LEFT_DIAMOND = 1
 
@@ -270,6 +274,11 @@ _SIGNATURES = {
          ctypes.c_char_p, ctypes.c_size_t],
     ),
     "qpeps_ctx_device_name": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_size_t]),
+    "qpeps_probe_append": (
+        ctypes.c_int,
+        [_VP, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double),
+         ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "qpeps_certify_c": (
         ctypes.c_int,
         [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_char_p,
@@ -604,6 +613,19 @@ class Context:
             entries[key] = {"tuning": out["tuning"], "device_ms": out["device_ms"]}
             path.write_text(json.dumps(entries, indent=1, sort_keys=True))
         return out
+
+    def probe_append(self, mode: int, candidates: int, parts: int, repeats: int = 3) -> float:
+        """Best device time (ms) of the scatter's memory pattern alone
+        (``qpeps_probe_append``): ``candidates`` pseudo-random 16-byte records
+        into ``parts`` partitions of 2048 slots by ``mode`` (PROBE_APPEND,
+        PROBE_STORE, PROBE_ATOMIC or PROBE_STREAM)."""
+        ms = ctypes.c_double()
+        err = ctypes.create_string_buffer(4096)
+        with self._lock:
+            rc = library().qpeps_probe_append(self._h, int(mode), int(candidates), int(parts), int(repeats),
+                                              ctypes.byref(ms), err, len(err))
+        _check(rc, err)
+        return ms.value
 
 
 def tuning_default() -> dict:

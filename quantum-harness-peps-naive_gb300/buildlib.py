@@ -34,7 +34,7 @@ NVCC_FLAGS = ARCH + [
     str(INCLUDE),
 ]
 LIB_SOURCES = ["qpeps_hash_kernels.cu", "qpeps_partition_kernels.cu", "qpeps_unit_kernels.cu", "qpeps_wide_kernels.cu",
-               "qpeps_engine.cu", "qpeps_noalloc.cu", "qpeps_tail_kernels.cu"]
+               "qpeps_engine.cu", "qpeps_noalloc.cu", "qpeps_tail_kernels.cu", "qpeps_probe_kernels.cu"]
 
 
 def nvcc() -> str:

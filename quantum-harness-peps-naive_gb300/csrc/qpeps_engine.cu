@@ -2798,6 +2798,60 @@ int qpeps_ctx_set_tuning(void* ctx, const qpeps_tuning* t, char* err, size_t err
   });
 }
 
+int qpeps_probe_append(void* ctx, uint32_t mode, uint64_t candidates, uint32_t parts, uint32_t repeats,
+                       double* best_ms, char* err, size_t err_len) {
+  return guarded(err, err_len, [&] {
+    if (!ctx) fail(QPEPS_ERR_INVALID, "null context");
+    if (mode > QPEPS_PROBE_STREAM) fail(QPEPS_ERR_INVALID, "probe mode must be 0..3");
+    if (parts == 0 || candidates == 0) fail(QPEPS_ERR_INVALID, "probe needs at least one partition and record");
+    Ctx& c = *static_cast<Ctx*>(ctx);
+    cuda_check(cudaSetDevice(c.device), "cudaSetDevice");
+    const u32 cap = partition_capacity(0);
+    const u32 cstride = (parts <= c.tune.spread_cursors_below) ? 8u : 1u;
+    const size_t region_bytes = (size_t)parts * cap * 16;
+    const size_t cursor_bytes = (size_t)parts * cstride * 4;
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    if (region_bytes + cursor_bytes + (1u << 20) > fr) fail(QPEPS_ERR_CAPACITY, "probe regions exceed free device memory");
+    void* regions = nullptr;
+    u32* cursors = nullptr;
+    unsigned long long* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto release = [&] {
+      if (regions) cudaFree(regions);
+      if (cursors) cudaFree(cursors);
+      if (sink) cudaFree(sink);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    };
+    try {
+      cuda_check(cudaMalloc(&regions, region_bytes), "probe regions");
+      cuda_check(cudaMalloc(reinterpret_cast<void**>(&cursors), cursor_bytes), "probe cursors");
+      cuda_check(cudaMalloc(reinterpret_cast<void**>(&sink), sizeof(unsigned long long)), "probe sink");
+      cuda_check(cudaEventCreate(&e0), "event");
+      cuda_check(cudaEventCreate(&e1), "event");
+      double best = 1e300;
+      for (uint32_t r = 0; r <= std::max(1u, repeats); ++r) {
+        cuda_check(cudaMemsetAsync(cursors, 0, cursor_bytes, c.stream), "clear probe cursors");
+        cuda_check(cudaEventRecord(e0, c.stream), "event");
+        cuda_check(launch_append_probe(mode, candidates, parts, cap, regions, cursors, cstride, c.sms, 0x9e37ull * (r + 1),
+                                       sink, c.stream),
+                   "probe kernel");
+        cuda_check(cudaEventRecord(e1, c.stream), "event");
+        cuda_check(cudaStreamSynchronize(c.stream), "probe synchronize");
+        float ms = 0;
+        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event time");
+        if (r) best = std::min(best, (double)ms);
+      }
+      if (best_ms) *best_ms = best;
+    } catch (...) {
+      release();
+      throw;
+    }
+    release();
+  });
+}
+
 int qpeps_autotune(void* ctx, uint32_t n, uint32_t repeats, qpeps_tuning* best, double* best_device_ms, char* err,
                    size_t err_len) {
   return guarded(err, err_len, [&] {

@@ -138,6 +138,12 @@ cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const Frontier
 cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                         const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
                                         cudaStream_t stream);
+// Access-pattern probe (qpeps_probe_append): `total` pseudo-random 16-byte
+// records into `parts` partitions of `cap` slots (cap a power of two) by mode
+// 0 append (cursor atomic + store), 1 store only, 2 atomic only, 3 stream.
+cudaError_t launch_append_probe(uint32_t mode, uint64_t total, uint32_t parts, uint32_t cap, void* regions,
+                                uint32_t* cursors, uint32_t cursor_stride, int sms, uint64_t seed,
+                                unsigned long long* sink, cudaStream_t stream);
 // Explicit-C frontier step through the same 128-bit partitions: the number of
 // (boundary entry, matching transition) pairs into `scalars->terms`, and
 // every such pair as one candidate (merged by launch_wide_partition_merge
