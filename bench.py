@@ -374,6 +374,10 @@ def run_ours(args):
         "scatter_ms_per_step": d["scatter_kernel_ms"],
         "merge_ms_per_step": d["merge_kernel_ms"],
         "step_ms_per_step": d["device_ms"],
+        # Successor candidates per step, and per second of scatter-kernel time
+        # (summed over concurrent lanes, so a per-kernel rate).
+        "candidates_per_step": d["candidates"],
+        "scatter_candidates_per_s": d["candidates"] / max(d["scatter_kernel_ms"] / 1e3, 1e-12),
     }
     if d["exact_weights"]:
         dtype = f"u{d['key_bits']} keys + exact u64 weights (2x u32 words), host-side CRT bookkeeping"
