@@ -48,25 +48,29 @@ __global__ void __launch_bounds__(kProbeBlock) append_probe_kernel(u64 total, u3
                                                                   unsigned long long* __restrict__ sink) {
   const u64 policy = probe_keep_policy();
   const u64 limit = (u64)parts * cap;
+  // Record i = warp base + k * 32 + lane: a warp's k-th store instruction
+  // covers 32 consecutive records (coalesced in mode 3).
+  const u64 lane = threadIdx.x & 31;
+  const u64 warp = ((u64)blockIdx.x * kProbeBlock + threadIdx.x) >> 5;
   const u64 stride = (u64)gridDim.x * kProbeBlock * kProbeIlp;
   unsigned long long acc = 0;
-  for (u64 base = ((u64)blockIdx.x * kProbeBlock + threadIdx.x) * kProbeIlp; base < total; base += stride) {
+  for (u64 base = warp * 32 * kProbeIlp + lane; base < total; base += stride) {
     u64 key[kProbeIlp];
     u32 part[kProbeIlp], pos[kProbeIlp];
 #pragma unroll
     for (int k = 0; k < kProbeIlp; ++k) {
-      key[k] = mix64(base + k + seed);
+      key[k] = mix64(base + 32 * k + seed);
       part[k] = (u32)(((key[k] >> 32) * (u64)parts) >> 32);
       pos[k] = 0;
     }
     if constexpr (MODE == 0 || MODE == 2) {
 #pragma unroll
       for (int k = 0; k < kProbeIlp; ++k)
-        if (base + k < total) pos[k] = atomicAdd(&cursors[(u64)part[k] * cstride], 1u);
+        if (base + 32 * k < total) pos[k] = atomicAdd(&cursors[(u64)part[k] * cstride], 1u);
     }
 #pragma unroll
     for (int k = 0; k < kProbeIlp; ++k) {
-      const u64 i = base + k;
+      const u64 i = base + 32 * k;
       if (i >= total) continue;
       if constexpr (MODE == 0) {
         if (pos[k] < cap) probe_store(regions + (u64)part[k] * cap + pos[k], key[k], i, policy);
