@@ -437,6 +437,22 @@ def run_ours(args):
         }
         if args.same_workload_n:
             line["same_workload"] = same_workload_pair(pkg, ctx, args.same_workload_n, threads)
+    if world == 1 and d["merge"] == 2 and d["key_bits"] == 64 and not args.no_pattern_probe:
+        # The scatter's access pattern alone on this device (random 16-byte
+        # appends into hash partitions, one cursor atomic each), measured
+        # after the timed region: the time the step's candidates need at that
+        # rate bounds the merge step from below, whatever the DRAM bandwidth.
+        cand = 512 << 20
+        fill = float(tuning.get("partition_fill", 0.75))
+        parts = int(cand / (fill * 2048)) + 1
+        rate = cand / (ctx.probe_append(pkg.PROBE_APPEND, cand, parts, repeats=3) * 1e-3)
+        bound_ms = d["candidates"] / rate * 1e3
+        line["scatter_pattern"] = {
+            "pattern": "random 16-byte appends into hash partitions of 2048 slots, one cursor atomic each",
+            "probe_records": cand, "probe_partitions": parts, "probe_records_per_s": rate,
+            "candidates_per_step": d["candidates"], "pattern_bound_ms_per_step": bound_ms,
+            "step_ms_per_step": d["device_ms"], "frac": bound_ms / max(d["device_ms"], 1e-12),
+        }
     ctx.close()
     if world == 1 and args.dfs_check:
         # The DFS bitboard oracle (src/dfs_bitmask.rs:67-340, restated in C++)
@@ -706,6 +722,8 @@ def main():
                     help="time the partition scatter's memory pattern alone instead of the Q(N) step")
     ap.add_argument("--probe-candidates", type=int, nargs="+", default=[64 << 20, 512 << 20])
     ap.add_argument("--probe-fill", type=float, default=0.75)
+    ap.add_argument("--no-pattern-probe", action="store_true",
+                    help="leave the scatter-pattern probe out of the Q(N) line")
     ap.add_argument("--explicit", type=int, default=0,
                     help="time the explicit-C site frontier at this N instead of the Q(N) step")
     ap.add_argument("--explicit-order", choices=["row", "diamond"], default="diamond")
