@@ -673,7 +673,8 @@ def run_probe(args):
         parts = max(1, int(cand / (args.probe_fill * 2048)) + 1)
         row = {"candidates": cand, "parts": parts, "fill": args.probe_fill}
         for name, mode in (("append", pkg.PROBE_APPEND), ("store_only", pkg.PROBE_STORE),
-                           ("atomic_only", pkg.PROBE_ATOMIC), ("stream", pkg.PROBE_STREAM)):
+                           ("atomic_only", pkg.PROBE_ATOMIC), ("stream", pkg.PROBE_STREAM),
+                           ("append_plain", pkg.PROBE_APPEND_PLAIN)):
             ms = ctx.probe_append(mode, cand, parts, repeats=args.steps)
             row[name] = {"ms": ms, "records_per_s": cand / (ms * 1e-3), "gb_per_s": cand * 16 / (ms * 1e-3) / 1e9}
         cases.append(row)

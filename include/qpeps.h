@@ -280,12 +280,14 @@ int qpeps_ctx_device_name(void* ctx, char* out, size_t len);
  * `mode`: QPEPS_PROBE_APPEND (one cursor atomic takes each record's slot, as
  * in the scatter), QPEPS_PROBE_STORE (stores to random slots, no atomic),
  * QPEPS_PROBE_ATOMIC (the atomics, no store), QPEPS_PROBE_STREAM (coalesced
- * stores). `best_ms`: the best CUDA-event time of `repeats` launches after
- * one untimed launch. Needs parts * 32 KiB of free device memory. */
+ * stores), QPEPS_PROBE_APPEND_PLAIN (the append without the scatter's L2 keep
+ * hint). `best_ms`: the best CUDA-event time of `repeats` launches after one
+ * untimed launch. Needs parts * 32 KiB of free device memory. */
 #define QPEPS_PROBE_APPEND 0
 #define QPEPS_PROBE_STORE 1
 #define QPEPS_PROBE_ATOMIC 2
 #define QPEPS_PROBE_STREAM 3
+#define QPEPS_PROBE_APPEND_PLAIN 4
 int qpeps_probe_append(void* ctx, uint32_t mode, uint64_t candidates, uint32_t parts, uint32_t repeats,
                        double* best_ms, char* err, size_t err_len);
 

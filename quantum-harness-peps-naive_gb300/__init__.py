@@ -165,6 +165,7 @@ PROBE_APPEND = 0
 PROBE_STORE = 1
 PROBE_ATOMIC = 2
 PROBE_STREAM = 3
+PROBE_APPEND_PLAIN = 4
 ORDER_ROW_MAJOR = 0
 ORDER_TOP_LEFT_DIAMOND = 1
 
@@ -618,7 +619,7 @@ class Context:
         """Best device time (ms) of the scatter's memory pattern alone
         (``qpeps_probe_append``): ``candidates`` pseudo-random 16-byte records
         into ``parts`` partitions of 2048 slots by ``mode`` (PROBE_APPEND,
-        PROBE_STORE, PROBE_ATOMIC or PROBE_STREAM)."""
+        PROBE_STORE, PROBE_ATOMIC, PROBE_STREAM or PROBE_APPEND_PLAIN)."""
         ms = ctypes.c_double()
         err = ctypes.create_string_buffer(4096)
         with self._lock:

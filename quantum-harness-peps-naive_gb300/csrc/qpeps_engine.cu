@@ -2802,7 +2802,7 @@ int qpeps_probe_append(void* ctx, uint32_t mode, uint64_t candidates, uint32_t p
                        double* best_ms, char* err, size_t err_len) {
   return guarded(err, err_len, [&] {
     if (!ctx) fail(QPEPS_ERR_INVALID, "null context");
-    if (mode > QPEPS_PROBE_STREAM) fail(QPEPS_ERR_INVALID, "probe mode must be 0..3");
+    if (mode > QPEPS_PROBE_APPEND_PLAIN) fail(QPEPS_ERR_INVALID, "probe mode must be 0..4");
     if (parts == 0 || candidates == 0) fail(QPEPS_ERR_INVALID, "probe needs at least one partition and record");
     Ctx& c = *static_cast<Ctx*>(ctx);
     cuda_check(cudaSetDevice(c.device), "cudaSetDevice");

@@ -10,9 +10,10 @@
 //   mode 1  store only: the same records to a pseudo-random slot of the same
 //           partition, no atomic;
 //   mode 2  atomic only: the cursor atomics of mode 0, no store;
-//   mode 3  stream: the records stored in index order (coalesced).
+//   mode 3  stream: the records stored in index order (coalesced);
+//   mode 4  append as mode 0 with plain stores (no L2 hint).
 //
-// Every store lands inside `parts * cap` records: modes 0 and 2 skip a slot
+// Every store lands inside `parts * cap` records: modes 0, 2 and 4 skip a slot
 // at or beyond `cap` (a full partition), mode 1 masks the slot with cap - 1
 // (cap a power of two), mode 3 runs only while the index is below
 // parts * cap.
@@ -63,7 +64,7 @@ __global__ void __launch_bounds__(kProbeBlock) append_probe_kernel(u64 total, u3
       part[k] = (u32)(((key[k] >> 32) * (u64)parts) >> 32);
       pos[k] = 0;
     }
-    if constexpr (MODE == 0 || MODE == 2) {
+    if constexpr (MODE == 0 || MODE == 2 || MODE == 4) {
 #pragma unroll
       for (int k = 0; k < kProbeIlp; ++k)
         if (base + 32 * k < total) pos[k] = atomicAdd(&cursors[(u64)part[k] * cstride], 1u);
@@ -78,6 +79,8 @@ __global__ void __launch_bounds__(kProbeBlock) append_probe_kernel(u64 total, u3
         probe_store(regions + (u64)part[k] * cap + ((u32)key[k] & (cap - 1)), key[k], i, policy);
       } else if constexpr (MODE == 2) {
         acc += pos[k];
+      } else if constexpr (MODE == 4) {
+        if (pos[k] < cap) regions[(u64)part[k] * cap + pos[k]] = make_ulonglong2(key[k], i);
       } else {
         if (i < limit) probe_store(regions + i, key[k], i, policy);
       }
@@ -93,7 +96,7 @@ __global__ void __launch_bounds__(kProbeBlock) append_probe_kernel(u64 total, u3
 cudaError_t launch_append_probe(uint32_t mode, uint64_t total, uint32_t parts, uint32_t cap, void* regions,
                                 uint32_t* cursors, uint32_t cursor_stride, int sms, uint64_t seed,
                                 unsigned long long* sink, cudaStream_t stream) {
-  if (parts == 0 || cap == 0 || (cap & (cap - 1)) || mode > 3 || cursor_stride == 0) return cudaErrorInvalidValue;
+  if (parts == 0 || cap == 0 || (cap & (cap - 1)) || mode > 4 || cursor_stride == 0) return cudaErrorInvalidValue;
   if (total == 0) return cudaSuccess;
   const u64 want = (total + (u64)kProbeBlock * kProbeIlp - 1) / ((u64)kProbeBlock * kProbeIlp);
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(want, (u64)sms * 8));
@@ -102,7 +105,8 @@ cudaError_t launch_append_probe(uint32_t mode, uint64_t total, uint32_t parts, u
     case 0: append_probe_kernel<0><<<grid, kProbeBlock, 0, stream>>>(total, parts, cap, r, cursors, cursor_stride, seed, sink); break;
     case 1: append_probe_kernel<1><<<grid, kProbeBlock, 0, stream>>>(total, parts, cap, r, cursors, cursor_stride, seed, sink); break;
     case 2: append_probe_kernel<2><<<grid, kProbeBlock, 0, stream>>>(total, parts, cap, r, cursors, cursor_stride, seed, sink); break;
-    default: append_probe_kernel<3><<<grid, kProbeBlock, 0, stream>>>(total, parts, cap, r, cursors, cursor_stride, seed, sink); break;
+    case 3: append_probe_kernel<3><<<grid, kProbeBlock, 0, stream>>>(total, parts, cap, r, cursors, cursor_stride, seed, sink); break;
+    default: append_probe_kernel<4><<<grid, kProbeBlock, 0, stream>>>(total, parts, cap, r, cursors, cursor_stride, seed, sink); break;
   }
   return cudaGetLastError();
 }
