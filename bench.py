@@ -445,14 +445,18 @@ def run_ours(args):
         cand = 512 << 20
         fill = float(tuning.get("partition_fill", 0.75))
         parts = int(cand / (fill * 2048)) + 1
-        rate = cand / (ctx.probe_append(pkg.PROBE_APPEND, cand, parts, repeats=3) * 1e-3)
-        bound_ms = d["candidates"] / rate * 1e3
-        line["scatter_pattern"] = {
-            "pattern": "random 16-byte appends into hash partitions of 2048 slots, one cursor atomic each",
-            "probe_records": cand, "probe_partitions": parts, "probe_records_per_s": rate,
-            "candidates_per_step": d["candidates"], "pattern_bound_ms_per_step": bound_ms,
-            "step_ms_per_step": d["device_ms"], "frac": bound_ms / max(d["device_ms"], 1e-12),
-        }
+        try:
+            rate = cand / (ctx.probe_append(pkg.PROBE_APPEND, cand, parts, repeats=3) * 1e-3)
+        except pkg.ContractionError as e:  # e.g. too little free device memory for the probe's regions
+            line["scatter_pattern"] = {"unavailable": e.message}
+        else:
+            bound_ms = d["candidates"] / rate * 1e3
+            line["scatter_pattern"] = {
+                "pattern": "random 16-byte appends into hash partitions of 2048 slots, one cursor atomic each",
+                "probe_records": cand, "probe_partitions": parts, "probe_records_per_s": rate,
+                "candidates_per_step": d["candidates"], "pattern_bound_ms_per_step": bound_ms,
+                "step_ms_per_step": d["device_ms"], "frac": bound_ms / max(d["device_ms"], 1e-12),
+            }
     ctx.close()
     if world == 1 and args.dfs_check:
         # The DFS bitboard oracle (src/dfs_bitmask.rs:67-340, restated in C++)
