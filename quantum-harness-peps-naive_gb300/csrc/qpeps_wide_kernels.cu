@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 
 #include "qpeps_device.cuh"
 #include "qpeps_internal.h"
@@ -37,7 +38,7 @@ constexpr u32 kWFull = 0xffffffffu;
 constexpr u128 kWEmpty = ~(u128)0;  // no boundary key sets all 128 bits (3n <= 126)
 
 template <int R>
-struct alignas(16) WCand {
+struct alignas(32) WCand {
   u128 key;
   u32 res[R];
 };
@@ -67,7 +68,10 @@ __device__ __forceinline__ u64 wl2_keep_policy() {
   return policy;
 }
 
-// A 32-byte candidate as two 16-byte stores (key; residue words).
+// A 32-byte candidate (key; residue words) moves as one 256-bit access
+// (sm_100 and later): one scattered store fills a whole 32-byte sector, where
+// two 16-byte stores would each leave it half written. Candidates sit at
+// 32-byte multiples of a cudaMalloc base, so every access is aligned.
 template <int R>
 __device__ __forceinline__ void wstore(WCand<R>* dst, const WCand<R>& c, u64 policy) {
   const u64 lo = (u64)c.key, hi = (u64)(c.key >> 64);
@@ -75,22 +79,23 @@ __device__ __forceinline__ void wstore(WCand<R>* dst, const WCand<R>& c, u64 pol
   if constexpr (R > 1) w01 |= (u64)c.res[R > 1 ? 1 : 0] << 32;
   if constexpr (R > 2) w23 = c.res[R > 2 ? 2 : 0];
   if constexpr (R > 3) w23 |= (u64)c.res[R > 3 ? 3 : 0] << 32;
-  char* d = reinterpret_cast<char*>(dst);
-  asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1, %2}, %3;" ::"l"(d), "l"(lo), "l"(hi), "l"(policy) : "memory");
-  asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1, %2}, %3;" ::"l"(d + 16), "l"(w01), "l"(w23), "l"(policy)
+  asm volatile("st.global.L2::cache_hint.v4.b64 [%0], {%1, %2, %3, %4}, %5;" ::"l"(dst), "l"(lo), "l"(hi), "l"(w01),
+               "l"(w23), "l"(policy)
                : "memory");
 }
 
 template <int R>
 __device__ __forceinline__ WCand<R> wload(const WCand<R>* src) {
-  const ulonglong2* s = reinterpret_cast<const ulonglong2*>(src);
-  const ulonglong2 a = __ldcs(s), b = __ldcs(s + 1);
+  u64 lo, hi, w01, w23;
+  asm volatile("ld.global.cs.v4.b64 {%0, %1, %2, %3}, [%4];"
+               : "=l"(lo), "=l"(hi), "=l"(w01), "=l"(w23)
+               : "l"(src));
   WCand<R> c;
-  c.key = ((u128)a.y << 64) | a.x;
-  c.res[0] = (u32)b.x;
-  if constexpr (R > 1) c.res[R > 1 ? 1 : 0] = (u32)(b.x >> 32);
-  if constexpr (R > 2) c.res[R > 2 ? 2 : 0] = (u32)b.y;
-  if constexpr (R > 3) c.res[R > 3 ? 3 : 0] = (u32)(b.y >> 32);
+  c.key = ((u128)hi << 64) | lo;
+  c.res[0] = (u32)w01;
+  if constexpr (R > 1) c.res[R > 1 ? 1 : 0] = (u32)(w01 >> 32);
+  if constexpr (R > 2) c.res[R > 2 ? 2 : 0] = (u32)w23;
+  if constexpr (R > 3) c.res[R > 3 ? 3 : 0] = (u32)(w23 >> 32);
   return c;
 }
 
@@ -483,7 +488,7 @@ uint32_t wide_key_partition_capacity() { return kWCap; }
 cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                           void* regions, uint32_t* cursors, StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
-  if (n_in > in.cap) return cudaErrorInvalidValue;
+  if (n_in > in.cap || reinterpret_cast<uintptr_t>(regions) % 32) return cudaErrorInvalidValue;
   switch (pc.residues) {
     case 1: return wide_scatter<1>(pc, in, n_in, n, regions, cursors, sc, stream);
     case 2: return wide_scatter<2>(pc, in, n_in, n, regions, cursors, sc, stream);
@@ -496,6 +501,7 @@ cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const Frontier
 cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                         const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
                                         cudaStream_t stream) {
+  if (reinterpret_cast<uintptr_t>(regions) % 32) return cudaErrorInvalidValue;  // 256-bit candidate loads
   switch (pc.residues) {
     case 1: return wide_merge<1>(pc, regions, cursors, out, n, write_out, sc, stream);
     case 2: return wide_merge<2>(pc, regions, cursors, out, n, write_out, sc, stream);
@@ -521,7 +527,7 @@ cudaError_t launch_frontier_partition_scatter(const PartitionCfg& pc, const Fron
                                               StepScalars* sc, cudaStream_t stream) {
   if (n_in == 0) return cudaSuccess;
   if (n_in > in.cap || pc.parts == 0 || pc.cap != (u32)kWCap || step.n_trans > (uint32_t)kFrontierMaxTrans ||
-      step.n_runs > (uint32_t)kFrontierMaxRuns)
+      step.n_runs > (uint32_t)kFrontierMaxRuns || reinterpret_cast<uintptr_t>(regions) % 32)
     return cudaErrorInvalidValue;
   const u64 want = (n_in + kWScatterBlock - 1) / kWScatterBlock;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(want, (u64)pc.sms * 8));
