@@ -229,7 +229,8 @@ typedef struct qpeps_tuning {
   uint32_t scatter_kind;         /* QPEPS_SCATTER_* */
   uint32_t parents_per_lane;     /* scatter: parents per lane per warp iteration, 2 or 4 */
   uint32_t merge_kind;           /* QPEPS_MERGEK_* */
-  uint32_t wide_merge;           /* 0 never, 1 always, 2 auto: 8192-slot merge CTAs, 4096-candidate partitions */
+  uint32_t wide_merge;           /* 0 never, 1 always, 2 auto: 8192-slot merge CTAs, 4096-candidate partitions;
+                                    3: 2048-slot merge CTAs, four per SM, 1024-candidate partitions */
   uint32_t wide_above_parts;     /* auto: 2048-candidate partition count above which merges go wide */
   uint32_t spread_cursors_below; /* partition counts up to which cursors get 32-byte spacing */
   uint32_t fold_weights;         /* 2 (default) = with the partitioned row merge and 13 <= N - k <= 21

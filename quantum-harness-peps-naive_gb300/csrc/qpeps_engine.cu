@@ -283,7 +283,8 @@ struct Ctx {
     uint32_t parents_per_lane = 4;              // partition scatter: 2 or 4
     uint32_t spread_cursors_below = 262144;     // pad cursors to 32 B when partitions <= this
     uint32_t wide_merge = 2;                    // 0 never, 1 always, 2 above wide_above_parts partitions:
-                                                // 8192-slot merge CTAs (4096-candidate partitions)
+                                                // 8192-slot merge CTAs (4096-candidate partitions);
+                                                // 3: 2048-slot CTAs, four per SM (1024-candidate partitions)
     uint32_t wide_above_parts = 524288;         // 2048-candidate partitions beyond which auto goes wide
     uint32_t scatter_kind = 1;                  // PartitionCfg::scatter_kind
     uint32_t merge_kind = 1;                    // PartitionCfg::merge_kind
@@ -615,7 +616,8 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   // 128-bit keys: their own scatter and merge (one shape, 1024-candidate partitions).
   const bool wkeys = p.key_bits == 128;
   const bool unit = partition && !wkeys && ctx.tune.scatter_kind == 3 && unit_scatter_supported(p.R);
-  const u32 wide = (!unit && !wkeys && want_wide && wide_merge_supported(p.R)) ? 1u : 0u;
+  const bool small = ctx.tune.wide_merge == 3;
+  const u32 wide = (!unit && !wkeys && wide_merge_supported(p.R)) ? (small ? 2u : want_wide ? 1u : 0u) : 0u;
   const u32 pcap = wkeys ? wide_key_partition_capacity() : partition_capacity(wide);
   double mean = ctx.partition_fill * pcap;
   double unit_target = ctx.tune.unit_target;
@@ -2600,7 +2602,7 @@ static Ctx::Tune tune_from(const qpeps_tuning& q) {
   if (q.slice_rows < 1 || q.slice_rows > 4) fail(QPEPS_ERR_INVALID, "slice_rows must be in [1, 4]");
   if (q.parents_per_lane != 2 && q.parents_per_lane != 4) fail(QPEPS_ERR_INVALID, "parents_per_lane must be 2 or 4");
   if (q.merge_kind > 1) fail(QPEPS_ERR_INVALID, "merge_kind must be 0 or 1");
-  if (q.wide_merge > 2) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1 or 2");
+  if (q.wide_merge > 3) fail(QPEPS_ERR_INVALID, "wide_merge must be 0, 1, 2 or 3");
   if (q.fold_weights > 2) fail(QPEPS_ERR_INVALID, "fold_weights must be 0, 1 or 2");
   if (!(q.partition_fill >= 0.3 && q.partition_fill <= 0.95))
     fail(QPEPS_ERR_INVALID, "partition_fill must be in [0.3, 0.95]");
@@ -2676,7 +2678,7 @@ static double autotune(Ctx& c, unsigned n, unsigned repeats, Ctx::Tune* best) {
       {{4, 2}, [](Ctx::Tune& t, double v) { t.parents_per_lane = (uint32_t)v; }},
       {{256, 128, 512}, [](Ctx::Tune& t, double v) { t.scatter_block = (uint32_t)v; }},
       {{1, 0}, [](Ctx::Tune& t, double v) { t.merge_kind = (uint32_t)v; }},
-      {{2, 0, 1}, [](Ctx::Tune& t, double v) { t.wide_merge = (uint32_t)v; }},
+      {{2, 0, 1, 3}, [](Ctx::Tune& t, double v) { t.wide_merge = (uint32_t)v; }},
       {{0.83, 0.9, 0.75}, [](Ctx::Tune& t, double v) { t.partition_fill = v; }},
       {{2, 1, 0}, [](Ctx::Tune& t, double v) { t.fold_weights = (uint32_t)v; }},
       {{QPEPS_MERGE_PARTITION, QPEPS_MERGE_HASH}, [](Ctx::Tune& t, double v) { t.merge_auto = (uint32_t)v; }},

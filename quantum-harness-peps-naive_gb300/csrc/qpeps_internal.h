@@ -109,7 +109,8 @@ struct PartitionCfg {
   uint32_t parents_per_lane = 2;  // scatter: parents per lane per iteration (2 or 4)
   uint32_t wide = 0;              // merge CTA shape: 0 = 512 threads, 4096-slot table, 2048 candidates,
                                   // two CTAs per SM; 1 = 1024 threads, 8192 slots, 4096 candidates,
-                                  // one CTA per SM (R <= 2 only: the table is 8 KiB x (8 + 8R) bytes)
+                                  // one CTA per SM (R <= 2 only: the table is 8 KiB x (8 + 8R) bytes);
+                                  // 2 = 256 threads, 2048 slots, 1024 candidates, four CTAs per SM (R <= 2)
   uint32_t scatter_kind = 1;      // scatter: 0 = shuffle search for each successor's parent,
                                   // 1 = per-warp shared-memory candidate window,
                                   // 2 = two-level (coarse buckets, then partitions; runs staged and

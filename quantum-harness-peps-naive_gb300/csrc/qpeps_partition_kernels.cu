@@ -1307,6 +1307,7 @@ constexpr int kScatterBlock = 256;
 // Merge CTA shapes: table slots H, candidate capacity H / 2.
 constexpr int kMergeBlock = 512, kMergeH = 4096;
 constexpr int kWideBlock = 1024, kWideH = 8192;
+constexpr int kSmallBlock = 256, kSmallH = 2048;  // four CTAs per SM
 
 template <int R, int H>
 constexpr size_t merge_smem() {
@@ -1393,6 +1394,8 @@ template <int R, typename Layout>
 cudaError_t merge_impl(const PartitionCfg& pc, const void* regions, const u32* cursors, const FrontierView& out,
                        Layout L, bool write_out, StepScalars* sc, cudaStream_t stream) {
   if constexpr (R <= 2) {
+    if (pc.wide == 2)
+      return merge_shape<R, kSmallBlock, kSmallH, Layout>(pc, 4, regions, cursors, out, L, write_out, sc, stream);
     if (pc.wide)
       return merge_shape<R, kWideBlock, kWideH, Layout>(pc, 1, regions, cursors, out, L, write_out, sc, stream);
   } else {
@@ -1430,7 +1433,7 @@ cudaError_t launch_serve_merge(const PartitionCfg& pc, const void* regions, cons
   if (pc.residues != 2) return cudaErrorInvalidValue;
   return merge_impl<2>(pc, regions, cursors, out, SlotLayout{slot_mask, slot_final}, true, sc, stream);
 }
-uint32_t partition_capacity(uint32_t wide) { return wide ? kWideH / 2 : kMergeH / 2; }
+uint32_t partition_capacity(uint32_t wide) { return wide == 2 ? kSmallH / 2 : wide ? kWideH / 2 : kMergeH / 2; }
 bool wide_merge_supported(int residues) { return residues >= 1 && residues <= 2; }
 
 size_t two_level_cursor_bytes(const PartitionCfg& pc) {

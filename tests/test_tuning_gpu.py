@@ -34,7 +34,7 @@ def tctx(qp):
 
 
 @pytest.mark.parametrize("scatter,ppl,merge,wide,fold", [
-    combo for combo in itertools.product((0, 1, 2, 3, 4), (2, 4), (0, 1), (0, 1), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
+    combo for combo in itertools.product((0, 1, 2, 3, 4), (2, 4), (0, 1), (0, 1, 3), (0, 1, 2)) if combo[2] == 1 or combo[4] == 0
 ])
 @pytest.mark.parametrize("compact", [0, 1])
 def test_every_kernel_shape_matches_oracle(tctx, oracle, scatter, ppl, merge, wide, fold, compact):
@@ -137,7 +137,7 @@ def test_low_partition_fill_and_slice_margin_are_exact(tctx, qp):
 
 
 @pytest.mark.parametrize("field,value", [
-    ("scatter_kind", 5), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 3), ("batch_lanes", 0),
+    ("scatter_kind", 5), ("parents_per_lane", 3), ("merge_kind", 5), ("wide_merge", 4), ("batch_lanes", 0),
     ("merge_compact", 2), ("unit_target", 100), ("unit_sample", 3), ("scatter_block", 300), ("merge_auto", 0),
     ("slice_rows", 5),
     ("partition_fill", 0.99), ("partition_fill", 0.1), ("slice_margin", 0.5), ("fold_weights", 3),
