@@ -105,17 +105,40 @@ struct State {
   u64 cols, dr, dl;
 };
 
+// Key layouts. u128 keys and u64 keys up to N = 21 hold the reference's
+// PackedBoundary layout (src/lib.rs:348-377): columns in bits [0, n), the
+// down-right diagonal signals in [n, 2n), the down-left ones in [2n, 3n).
+// A row step shifts the down-right signals up and the down-left ones down, so
+// every boundary after a row has dr bit 0 and dl bit n - 1 clear: only 3n - 2
+// bits are live. At N = 22 a u64 key holds exactly those (compact layout):
+// columns [0, 22), dr bits 1..21 in [22, 43), dl bits 0..20 in [43, 64).
+constexpr unsigned kRefU64MaxN = 21;  // widest board with the reference layout in a u64 key
+constexpr unsigned kU64MaxN = 22;     // widest board a u64 key holds (compact layout)
+
 template <typename K>
 __host__ __device__ __forceinline__ State unpack(K key, unsigned n, u64 mask) {
   State s;
   s.cols = (u64)key & mask;
+  if constexpr (sizeof(K) == 8) {
+    if (n > kRefU64MaxN) {
+      const u64 live = mask >> 1;
+      s.dr = (((u64)key >> n) & live) << 1;
+      s.dl = ((u64)key >> (2 * n - 1)) & live;
+      return s;
+    }
+  }
   s.dr = (u64)(key >> n) & mask;
   s.dl = (u64)(key >> (2 * n)) & mask;
   return s;
 }
 
+// dr bit 0 and dl bit n - 1 must be clear at N = 22 with u64 keys (true of
+// every boundary state: the empty one and every row successor).
 template <typename K>
 __host__ __device__ __forceinline__ K pack(u64 cols, u64 dr, u64 dl, unsigned n) {
+  if constexpr (sizeof(K) == 8) {
+    if (n > kRefU64MaxN) return (K)(cols | ((dr >> 1) << n) | (dl << (2 * n - 1)));
+  }
   return (K)cols | ((K)dr << n) | ((K)dl << (2 * n));
 }
 

@@ -615,7 +615,9 @@ static StepStatus merge_step(Ctx& ctx, const Plan& p, DevFrontier& f, bool site,
   // Class-grouped partitions (16-byte candidates, narrow merge CTAs).
   // 128-bit keys: their own scatter and merge (one shape, 1024-candidate partitions).
   const bool wkeys = p.key_bits == 128;
-  const bool unit = partition && !wkeys && ctx.tune.scatter_kind == 3 && unit_scatter_supported(p.R);
+  // (Its classes read the reference key layout: boards up to N = 21.)
+  const bool unit = partition && !wkeys && ctx.tune.scatter_kind == 3 && unit_scatter_supported(p.R) &&
+                    p.n <= kRefU64MaxN;
   const bool small = ctx.tune.wide_merge == 3;
   const u32 wide = (!unit && !wkeys && wide_merge_supported(p.R)) ? (small ? 2u : want_wide ? 1u : 0u) : 0u;
   const u32 pcap = wkeys ? wide_key_partition_capacity() : partition_capacity(wide);
@@ -869,7 +871,11 @@ static HostChunk chunk_from_items(const Plan& p, const std::vector<Item>& items,
   hc.res.resize((size_t)p.R * hc.count);
   for (u64 i = 0; i < hc.count; ++i) {
     if (kb == 8) {
-      const u64 k = (u64)items[i].key;
+      // Host items hold the reference layout in a u128; a u64 device key at
+      // N = 22 takes the compact layout.
+      const u64 mask = (1ull << p.n) - 1;
+      const State st = unpack<u128>(items[i].key, p.n, mask);
+      const u64 k = pack<u64>(st.cols, st.dr, st.dl, p.n);
       std::memcpy(&hc.keys[i * 8], &k, 8);
     } else {
       std::memcpy(&hc.keys[i * 16], &items[i].key, 16);
@@ -1112,7 +1118,9 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
   if (p.R < 1 || p.R > kMaxResidues) fail(QPEPS_ERR_INVALID, "residue count must be in 1..=4");
   if (o.residues && p.R < crt_plan(free_rows))
     fail(QPEPS_ERR_RANGE, "forced residue count does not certify N! for this N");
-  const unsigned narrow_max = p.grain == QPEPS_GRAIN_SITE ? 20 : 21;
+  // Row keys fit a u64 up to N = 22 (the compact layout at 22); the per-site
+  // form's mid-row key carries one more bit, the row signal at bit 3N.
+  const unsigned narrow_max = p.grain == QPEPS_GRAIN_SITE ? 20 : kU64MaxN;
   if (o.key_bits == 0)
     p.key_bits = n <= narrow_max ? 64 : 128;
   else if (o.key_bits == 64 || o.key_bits == 128)
@@ -1140,7 +1148,7 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
   else
     fail(QPEPS_ERR_INVALID, "unknown merge strategy");
   // The slice tail needs u64 keys and the compiled row operator.
-  const bool tail_ok = p.key_bits == 64 && p.grain == QPEPS_GRAIN_ROW && n >= 2;
+  const bool tail_ok = p.key_bits == 64 && p.grain == QPEPS_GRAIN_ROW && n >= 2 && n <= kRefU64MaxN;
   if (o.tail_row == 0)
     p.tail_row = n;  // auto: the merged row engine for every row (fastest measured through N=18)
   else
@@ -1149,9 +1157,11 @@ static Plan make_plan(Ctx& ctx, unsigned n, const qpeps_options& o, unsigned fre
   // two u32 planes carry each weight's words and the host derives the Rc
   // residues of the CRT bookkeeping from exact sums. Every row is certified
   // before it runs from the exact total of its input (run_chunks); with at
-  // most 20 free rows that holds by 20! < 2^63, with 21 (Q(21)) it is checked.
+  // most 20 free rows that holds by 20! < 2^63; with 21 or 22 it is checked
+  // (a row's total is at most its partial placements, for Q(22) far below
+  // 2^63 / 22).
   p.Rc = p.R;
-  if (ctx.tune.fold_weights == 2 && ctx.tune.merge_kind == 1 && p.R >= 2 && p.free_rows <= 21 &&
+  if (ctx.tune.fold_weights == 2 && ctx.tune.merge_kind == 1 && p.R >= 2 && p.free_rows <= 22 &&
       p.merge == QPEPS_MERGE_PARTITION && p.grain == QPEPS_GRAIN_ROW && p.key_bits == 64 && p.tail_row >= n) {
     p.w64 = true;
     p.R = 2;

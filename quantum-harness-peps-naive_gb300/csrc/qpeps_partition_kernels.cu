@@ -45,7 +45,13 @@ __device__ __forceinline__ unsigned pnth_set_bit(u64 m, int k) {
   return k < plo ? __fns(lo, 0, k + 1) : 32u + __fns(hi, 0, k - plo + 1);
 }
 
-constexpr u64 kEmptyKey = ~0ull;  // no u64 boundary key has bit 63 set (3n <= 63)
+// No u64 boundary key is all ones. Up to N = 21 bit 63 is clear (3n <= 63).
+// At N = 22 (compact layout, 64 live bits) all ones would need all 22 columns
+// set, so the last row placed, and all 21 live dr and all 21 live dl signals
+// set: 42 signals, where the queen of row i still has a dr signal on the board
+// only if its column is below i and a dl signal only if its column is at least
+// 22 - i, so at most 22 queens + the 10 of rows 12..21 give 32.
+constexpr u64 kEmptyKey = ~0ull;
 
 // Map a 64-bit hash uniformly onto [0, parts) (multiply-high).
 __device__ __forceinline__ u32 partition_of(u64 h, u32 parts) { return (u32)(((h >> 32) * (u64)parts) >> 32); }

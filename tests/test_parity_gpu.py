@@ -156,16 +156,16 @@ def _legal_prefix(n, k, seed):
             return cols
 
 
-@pytest.mark.parametrize("n,k", [(22, 7), (24, 9), (26, 11), (28, 13), (30, 15), (42, 30)])
-def test_boards_beyond_u64_keys_use_u128_keys_and_match_oracle(ctx, oracle, n, k):
-    # N >= 22: the packed boundary needs 3N > 64 bits, so keys are u128 (natural,
-    # not forced) and the merge is the partitioned one with 128-bit keys; the
-    # global table gives the same count. N = 42 is the widest board the
-    # reference accepts. The
-    # prefixes keep the oracle's frontier at up to about 0.4 M states.
+@pytest.mark.parametrize("n,k", [(22, 7), (23, 8), (24, 9), (26, 11), (28, 13), (30, 15), (42, 30)])
+def test_wide_boards_match_oracle(ctx, oracle, n, k):
+    # N = 22: the 3N - 2 live bits of a row key fill a u64 exactly (compact
+    # layout); N >= 23 needs u128 keys (natural, not forced), merged through
+    # the partitioned merge with 128-bit keys. N = 42 is the widest board the
+    # reference accepts. The prefixes keep the oracle's frontier at up to
+    # about 0.4 M states.
     prefix = _legal_prefix(n, k, 1000 + n)
     count, res = ctx.count_with_stats(n, prefix)
-    assert res.device["key_bits"] == 128
+    assert res.device["key_bits"] == (64 if n == 22 else 128)
     # residues certify (N - k)!: completions place N - k queens in distinct columns
     bound, prod, want_r = math.factorial(n - k), 1, 0
     for p in (2147483647, 2147483629, 2147483587, 2147483579):
@@ -374,3 +374,26 @@ def test_merge_counts_the_next_rows_terms(ctx, oracle, n, key_bits):
     d = g.device
     device_rows = n - d["slice_depth"]
     assert d["gpu_launches"] == d["batches"] * (1 + 2 * device_rows)
+
+
+@pytest.mark.parametrize("k,seed", [(6, 5), (7, 1022), (8, 9)])
+def test_n22_compact_u64_keys_equal_u128_keys(ctx, qp, oracle, k, seed):
+    """At N = 22 the u64 key drops the two always-clear diagonal bits (dr bit
+    0, dl bit 21): every row of a prefix contraction equals the 128-bit-key
+    run's and the global table's, the weights travel as exact 64-bit words,
+    and a CUDA-graph replay repeats it."""
+    prefix = _legal_prefix(22, k, seed)
+    c64, r64 = ctx.count_with_stats(22, prefix, use_graph=0)
+    c128, r128 = ctx.count_with_stats(22, prefix, key_bits=128)
+    ctab, rtab = ctx.count_with_stats(22, prefix, merge=qp.MERGE_HASH)
+    assert r64.device["key_bits"] == 64 and r64.device["exact_weights"]
+    assert r128.device["key_bits"] == 128 and rtab.device["key_bits"] == 64
+    assert c64 == c128 == ctab
+    assert r64.peak_states == r128.peak_states == rtab.peak_states
+    assert r64.device["entries_out"] == r128.device["entries_out"] == rtab.device["entries_out"]
+    g1, _ = ctx.count_with_stats(22, prefix, use_graph=1)
+    g2, rg = ctx.count_with_stats(22, prefix, use_graph=1)
+    assert g1 == g2 == c64
+    if k >= 7:
+        want = oracle.contract(22, backend=oracle.PARALLEL_SORT_REDUCE, threads=8, symmetry=False, prefix=prefix)
+        assert c64 == want["count"] and r64.peak_states == want["peak_states"]
