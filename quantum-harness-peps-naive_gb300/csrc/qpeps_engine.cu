@@ -1998,7 +1998,11 @@ static void contract_impl(Ctx& ctx, unsigned n, const qpeps_options& o, const ui
   if (o.slice_depth == 0 && out.plan.grain == QPEPS_GRAIN_ROW && row0 < n && !items.empty()) {
     const double per_state = 2.0 * (double)entry_bytes(out.plan) + 1.25 * (double)cand_bytes(out.plan);
     const double cap_states = 0.8 * (double)out.plan.budget / per_state;
-    double est_total = serve_estimate(n, k);
+    // A placed prefix's frontier is estimated from the average over all
+    // prefixes of its depth; central prefixes run to several times that (N=22:
+    // 1.8-2.6x at depth 3), and an underestimate costs host spills at the peak
+    // rows, so prefixes are sliced on four times the estimate.
+    double est_total = serve_estimate(n, k) * (k ? 4.0 : 1.0);
     while (est_total > cap_states && row0 + 2 < n) {
       // Slices are uneven (centre columns carry more states): tuned margin.
       const double est_item = est_total / (double)items.size() * ctx.tune.slice_margin;
