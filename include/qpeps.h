@@ -114,7 +114,8 @@ typedef struct qpeps_options {
   uint32_t granularity;          /* QPEPS_GRAIN_* */
   uint32_t merge;                /* QPEPS_MERGE_* */
   uint32_t residues;             /* 0 = shortest prime prefix with product > N!, else 1..4 */
-  uint32_t key_bits;             /* 0 = narrowest that fits, 64 or 128 to force */
+  uint32_t key_bits;             /* 0 = narrowest that fits (64 up to N = 22, where the row key drops the
+                                    two diagonal bits every row step clears), 64 or 128 to force */
   uint32_t slice_depth;          /* 0 = auto, else rows enumerated on the host (>= 1) */
   uint32_t symmetry;             /* 1 = first-row vertical-reflection orbits (reference default) */
   uint32_t collect_layers;       /* 1 = fill per-row metrics */

@@ -1,4 +1,4 @@
-// Partitioned merge for 128-bit boundary keys (boards with N >= 22, or
+// Partitioned merge for 128-bit boundary keys (boards with N >= 23, or
 // key_bits = 128 forced): the same two streaming passes per row as the u64
 // path, with 32-byte candidates and a shared-memory table of 128-bit keys.
 //
