@@ -115,20 +115,21 @@ struct State {
 constexpr unsigned kRefU64MaxN = 21;  // widest board with the reference layout in a u64 key
 constexpr unsigned kU64MaxN = 22;     // widest board a u64 key holds (compact layout)
 
+// For u64 keys both layouts are one formula with c = 1 (compact) or 0
+// (reference): no branch in the kernels' inner loops.
 template <typename K>
 __host__ __device__ __forceinline__ State unpack(K key, unsigned n, u64 mask) {
   State s;
   s.cols = (u64)key & mask;
   if constexpr (sizeof(K) == 8) {
-    if (n > kRefU64MaxN) {
-      const u64 live = mask >> 1;
-      s.dr = (((u64)key >> n) & live) << 1;
-      s.dl = ((u64)key >> (2 * n - 1)) & live;
-      return s;
-    }
+    const unsigned c = n > kRefU64MaxN ? 1u : 0u;
+    const u64 live = mask >> c;
+    s.dr = (((u64)key >> n) & live) << c;
+    s.dl = ((u64)key >> (2 * n - c)) & live;
+  } else {
+    s.dr = (u64)(key >> n) & mask;
+    s.dl = (u64)(key >> (2 * n)) & mask;
   }
-  s.dr = (u64)(key >> n) & mask;
-  s.dl = (u64)(key >> (2 * n)) & mask;
   return s;
 }
 
@@ -137,9 +138,11 @@ __host__ __device__ __forceinline__ State unpack(K key, unsigned n, u64 mask) {
 template <typename K>
 __host__ __device__ __forceinline__ K pack(u64 cols, u64 dr, u64 dl, unsigned n) {
   if constexpr (sizeof(K) == 8) {
-    if (n > kRefU64MaxN) return (K)(cols | ((dr >> 1) << n) | (dl << (2 * n - 1)));
+    const unsigned c = n > kRefU64MaxN ? 1u : 0u;
+    return (K)(cols | ((dr >> c) << n) | (dl << (2 * n - c)));
+  } else {
+    return (K)cols | ((K)dr << n) | ((K)dl << (2 * n));
   }
-  return (K)cols | ((K)dr << n) | ((K)dl << (2 * n));
 }
 
 // Compiled row successor (src/lib.rs:600-638 after certification): place the
