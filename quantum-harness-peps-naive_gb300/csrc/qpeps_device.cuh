@@ -116,16 +116,19 @@ constexpr unsigned kRefU64MaxN = 21;  // widest board with the reference layout 
 constexpr unsigned kU64MaxN = 22;     // widest board a u64 key holds (compact layout)
 
 // For u64 keys both layouts are one formula with c = 1 (compact) or 0
-// (reference): no branch in the kernels' inner loops.
+// (reference) and the same operations as the reference layout alone: the
+// down-right field starts at bit n - c (its always-clear bit 0 lands on the
+// top column bit and is masked off when read back) and the down-left field at
+// 2n - c (its always-clear top bit leaves the word). No branch, and no extra
+// operation per key, in the kernels' inner loops.
 template <typename K>
 __host__ __device__ __forceinline__ State unpack(K key, unsigned n, u64 mask) {
   State s;
   s.cols = (u64)key & mask;
   if constexpr (sizeof(K) == 8) {
     const unsigned c = n > kRefU64MaxN ? 1u : 0u;
-    const u64 live = mask >> c;
-    s.dr = (((u64)key >> n) & live) << c;
-    s.dl = ((u64)key >> (2 * n - c)) & live;
+    s.dr = ((u64)key >> (n - c)) & (mask & ~(u64)c);
+    s.dl = ((u64)key >> (2 * n - c)) & mask;
   } else {
     s.dr = (u64)(key >> n) & mask;
     s.dl = (u64)(key >> (2 * n)) & mask;
@@ -139,7 +142,7 @@ template <typename K>
 __host__ __device__ __forceinline__ K pack(u64 cols, u64 dr, u64 dl, unsigned n) {
   if constexpr (sizeof(K) == 8) {
     const unsigned c = n > kRefU64MaxN ? 1u : 0u;
-    return (K)(cols | ((dr >> c) << n) | (dl << (2 * n - c)));
+    return (K)(cols | (dr << (n - c)) | (dl << (2 * n - c)));
   } else {
     return (K)cols | ((K)dr << n) | ((K)dl << (2 * n));
   }
