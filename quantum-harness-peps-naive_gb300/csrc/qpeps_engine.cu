@@ -1268,20 +1268,31 @@ struct ExplicitRun {
 // that count, scatter, merge. Returns the count; the merged boundary's
 // scalars are left in ctx.h_sc. An overflowing partition makes the merge
 // write nothing, so the step is retried with smaller partitions.
+// `known_terms`: the step's match count when the previous step's merge
+// counted it (kTermsUnknown otherwise); on return, this step's merge count of
+// the next step's matches, if `next_dev` (the next step on the device) was
+// given and the merge counted them.
 static u64 explicit_partition_step(Ctx& ctx, const Plan& p, DevFrontier& f, const FrontierStepDev& st,
-                                   ExplicitRun& out) {
+                                   const FrontierStepDev* next_dev, u64& known_terms, ExplicitRun& out) {
   float ms = 0;
-  cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
-  cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
-  cuda_check(launch_frontier_count(view_of(p, ctx.front[0], f.cap), f.count, st, ctx.sms, ctx.d_sc, ctx.stream),
-             "frontier count kernel");
-  cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
-  out.launches += f.count ? 1 : 0;
-  sync_scalars(ctx);
-  cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
-  out.device_ms += ms;
-  const u64 terms = ctx.h_sc->terms;
-  if (terms == 0) return 0;  // the scalars read back say: no entries, zero weight
+  u64 terms = known_terms;
+  known_terms = kTermsUnknown;
+  if (terms == kTermsUnknown) {
+    cuda_check(cudaMemsetAsync(ctx.d_sc, 0, sizeof(StepScalars), ctx.stream), "clear step scalars");
+    cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
+    cuda_check(launch_frontier_count(view_of(p, ctx.front[0], f.cap), f.count, st, ctx.sms, ctx.d_sc, ctx.stream),
+               "frontier count kernel");
+    cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
+    out.launches += f.count ? 1 : 0;
+    sync_scalars(ctx);
+    cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]);
+    out.device_ms += ms;
+    terms = ctx.h_sc->terms;
+  }
+  if (terms == 0) {  // no entries, zero weight: what the caller reads back
+    std::memset(ctx.h_sc, 0, sizeof(StepScalars));
+    return 0;
+  }
   const u32 pcap = wide_key_partition_capacity();
   double mean = ctx.partition_fill * pcap;
   for (int attempt = 0;; ++attempt) {
@@ -1311,7 +1322,7 @@ static u64 explicit_partition_step(Ctx& ctx, const Plan& p, DevFrontier& f, cons
     cuda_check(cudaEventRecord(ctx.ev[0], ctx.stream), "event");
     cuda_check(launch_frontier_partition_scatter(pc, view, f.count, st, regions, cursors, ctx.d_sc, ctx.stream),
                "frontier scatter kernel");
-    cuda_check(launch_wide_partition_merge(pc, regions, cursors, view, 0, true, ctx.d_sc, ctx.stream),
+    cuda_check(launch_wide_partition_merge(pc, regions, cursors, view, 0, true, ctx.d_sc, ctx.stream, next_dev),
                "frontier merge kernel");
     cuda_check(cudaEventRecord(ctx.ev[1], ctx.stream), "event");
     out.launches += 2;
@@ -1326,6 +1337,7 @@ static u64 explicit_partition_step(Ctx& ctx, const Plan& p, DevFrontier& f, cons
       continue;
     }
     if (ctx.h_sc->error) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier: device capacity error");
+    if (next_dev && ctx.h_sc->next_terms_ok) known_terms = ctx.h_sc->next_terms;
     return terms;
   }
 }
@@ -1389,9 +1401,17 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
     f.count = 1;
   }
   LaunchCfg cfg{128, p.R, 256, ctx.sms};
+  // Pass 1 (host only): every site step's transitions and open-bond count, so
+  // that each step's merge can count the next step's matches on the device.
+  // An error found here is raised when the contraction reaches its step.
+  const size_t total = ordering.size();
+  std::vector<FrontierStepDev> steps(total);
+  std::vector<size_t> open_after(total, 0);
+  size_t fail_step = total;
+  int fail_code = QPEPS_OK;
+  std::string fail_msg;
   std::vector<unsigned> open;
-  u64 weight_res[kMaxResidues] = {0, 0, 0, 0};
-  for (size_t step = 0; step < ordering.size(); ++step) {
+  for (size_t step = 0; step < total && fail_step == total; ++step) {
     const FrontierSiteH& site = sites[ordering[step]];
     auto pos_in = [](const std::vector<unsigned>& v, unsigned id) -> int {
       auto it = std::lower_bound(v.begin(), v.end(), id);
@@ -1410,7 +1430,10 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
       char buf[96];
       std::snprintf(buf, sizeof buf, "explicit-C frontier exceeds 128 open bonds at site (%u,%u)", site.row,
                     site.column);
-      fail(QPEPS_ERR_RANGE, buf);
+      fail_step = step;
+      fail_code = QPEPS_ERR_RANGE;
+      fail_msg = buf;
+      break;
     }
     // Bonds that stay open keep their order: group them into runs that move
     // by one shift each.
@@ -1423,7 +1446,12 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
       if ((int)i == prev_old + 1 && j == prev_new + 1 && st.n_runs > 0) {
         st.run_mask[st.n_runs - 1] |= (u128)1 << i;
       } else {
-        if (st.n_runs == (uint32_t)kFrontierMaxRuns) fail(QPEPS_ERR_CAPACITY, "explicit-C frontier: too many bond runs");
+        if (st.n_runs == (uint32_t)kFrontierMaxRuns) {
+          fail_step = step;
+          fail_code = QPEPS_ERR_CAPACITY;
+          fail_msg = "explicit-C frontier: too many bond runs";
+          break;
+        }
         st.run_mask[st.n_runs] = (u128)1 << i;
         st.run_shift[st.n_runs] = j - (int)i;
         ++st.n_runs;
@@ -1453,27 +1481,52 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
       st.added[st.n_trans] = added;
       ++st.n_trans;
     }
+    if (fail_step < total) break;
+    steps[step] = st;
+    open_after[step] = next.size();
+    open.swap(next);
+  }
+  const bool ends_closed = open.empty();
+  // The partitioned merge unless the tuning asks for the global table, or a
+  // key could set all 128 bits (the partition tables' empty marker).
+  const bool partitioned = ctx.tune.merge_auto != QPEPS_MERGE_HASH;
+  FrontierStepDev* d_steps = nullptr;
+  if (partitioned && total > 1) {
+    buf_reserve(ctx, ctx.plan, total * sizeof(FrontierStepDev), p.budget, "explicit-C frontier steps");
+    d_steps = static_cast<FrontierStepDev*>(ctx.plan.ptr);
+    cuda_check(cudaMemcpyAsync(d_steps, steps.data(), total * sizeof(FrontierStepDev), cudaMemcpyHostToDevice,
+                               ctx.stream),
+               "frontier steps");
+    ctx.h2d_bytes += total * sizeof(FrontierStepDev);
+  }
+  // Pass 2: the device steps.
+  u64 weight_res[kMaxResidues] = {0, 0, 0, 0};
+  u64 known_terms = kTermsUnknown;
+  for (size_t step = 0; step < total; ++step) {
+    if (step == fail_step) fail(fail_code, fail_msg);
+    const FrontierStepDev& st = steps[step];
+    const size_t next_open = open_after[step];
     out.examined += (u128)f.count * 17;
-    // The partitioned merge unless the tuning asks for the global table, or
-    // a key could set all 128 bits (the partition tables' empty marker).
-    if (ctx.tune.merge_auto != QPEPS_MERGE_HASH && next.size() < 128) {
-      const u64 terms = explicit_partition_step(ctx, p, f, st, out);
+    if (partitioned && next_open < 128) {
+      const bool next_partitioned = step + 1 < total && step + 1 != fail_step && open_after[step + 1] < 128;
+      const FrontierStepDev* next_dev = (d_steps && next_partitioned) ? d_steps + step + 1 : nullptr;
+      const u64 terms = explicit_partition_step(ctx, p, f, st, next_dev, known_terms, out);
       out.accepted += terms;
       const u64 merged = ctx.h_sc->out_count;
       if (merged > support_limit) {
         out.peak_states = std::max<u64>(out.peak_states, support_limit + 1);
-        out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next.size());
+        out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next_open);
         out.contracted_sites = step;
         out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return;
       }
       f.count = merged;
       for (int r = 0; r < p.R; ++r) weight_res[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
-      open.swap(next);
       out.peak_states = std::max<u64>(out.peak_states, merged);
-      out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, open.size());
+      out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next_open);
       continue;
     }
+    known_terms = kTermsUnknown;
     // Every incoming leg of a site is a bond of an earlier site or a board
     // edge in both orders, so at most two C entries match a key.
     const u64 need = std::max<u64>(f.count * 2, 1);
@@ -1502,18 +1555,17 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
     const u64 merged = ctx.h_sc->out_count;
     if (merged > support_limit) {
       out.peak_states = std::max<u64>(out.peak_states, support_limit + 1);
-      out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next.size());
+      out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next_open);
       out.contracted_sites = step;
       out.elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
       return;
     }
     f.count = merged;
     for (int r = 0; r < p.R; ++r) weight_res[r] = ctx.h_sc->weight_sum[r] % kPrimes[r];
-    open.swap(next);
     out.peak_states = std::max<u64>(out.peak_states, merged);
-    out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, open.size());
+    out.peak_open_bonds = std::max<u64>(out.peak_open_bonds, next_open);
   }
-  if (!open.empty()) fail(QPEPS_ERR_INVALID, "explicit-C contraction ended with uncontracted virtual bonds");
+  if (!ends_closed) fail(QPEPS_ERR_INVALID, "explicit-C contraction ended with uncontracted virtual bonds");
   // No bond is open: the boundary is the single key 0 (or empty) and its
   // weight is the count.
   if (f.count > 1) fail(QPEPS_ERR_INVALID, "explicit-C contraction ended with more than one closed boundary");

@@ -136,9 +136,13 @@ size_t candidate_bytes(int residues);
 uint32_t wide_key_partition_capacity();
 cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const FrontierView& in, uint64_t n_in, unsigned n,
                                           void* regions, uint32_t* cursors, StepScalars* scalars, cudaStream_t stream);
+// With n > 0 (row keys) the merge counts the written boundary's successor
+// terms at the next row; with n = 0 and `next_step` (explicit-C bond keys, a
+// device copy of the next site step) it counts the boundary's matches there.
+// Either count lands in scalars->next_terms with next_terms_ok set.
 cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                         const FrontierView& out, unsigned n, bool write_out, StepScalars* scalars,
-                                        cudaStream_t stream);
+                                        cudaStream_t stream, const FrontierStepDev* next_step = nullptr);
 // Access-pattern probe (qpeps_probe_append): `total` pseudo-random 16-byte
 // records into `parts` partitions of `cap` slots (cap a power of two) by mode
 // 0 append (cursor atomic + store), 1 store only, 2 atomic only, 3 stream.

@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
                                                           const u32* __restrict__ cursors, u32 cstride, u32 parts,
                                                           u128* __restrict__ keys_out, u32* __restrict__ res_out,
                                                           u64 out_stride, unsigned n, int write_out,
+                                                          const FrontierStepDev* __restrict__ next_step,
                                                           StepScalars* __restrict__ sc) {
   static_assert((H & (H - 1)) == 0 && H >= 2 * CAP && CAP % BLOCK == 0, "merge shape");
   constexpr int kLogH = 31 - __builtin_clz(H);
@@ -266,8 +267,20 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
   u32* s_list = reinterpret_cast<u32*>(smem_raw + (size_t)H * 16 + (size_t)R * H * 8);            // [CAP]
   __shared__ u32 s_nused, s_n;
   __shared__ unsigned long long s_base;
+  // Explicit-C frontier: the next site step's transitions, to count the
+  // written boundary's matches there (its successor terms).
+  __shared__ u128 s_req_mask[kFrontierMaxTrans], s_req_value[kFrontierMaxTrans];
+  __shared__ u32 s_next_trans;
   const int lane = threadIdx.x & 31;
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
+  const bool count_next = write_out && (n > 0 || next_step != nullptr);
+  if (next_step != nullptr) {
+    if (threadIdx.x == 0) s_next_trans = min(next_step->n_trans, (u32)kFrontierMaxTrans);
+    for (int t = threadIdx.x; t < kFrontierMaxTrans; t += BLOCK) {
+      s_req_mask[t] = next_step->req_mask[t];
+      s_req_value[t] = next_step->req_value[t];
+    }
+  }
   const u64 mask = (n >= 64) ? ~0ull : ((1ull << n) - 1);
   unsigned long long wsum[R], fsum[R], fstates = 0;
   unsigned long long nterms = 0;  // the written boundary's successor terms at the next row (n > 0)
@@ -371,6 +384,8 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
       if (n) {
         const State st = unpack<u128>(key, n, mask);
         nterms += __popcll(~(st.cols | st.dr | st.dl) & mask);
+      } else if (next_step != nullptr) {
+        for (u32 t = 0; t < s_next_trans; ++t) nterms += (key & s_req_mask[t]) == s_req_value[t];
       }
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -394,7 +409,7 @@ __global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __res
   }
   const unsigned long long t = wblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
-  if (write_out && n) {
+  if (count_next) {
     const unsigned long long nt = wblock_sum<BLOCK>(nterms);
     if (threadIdx.x == 0 && nt) atomicAdd(&sc->next_terms, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->next_terms_ok = 1u;
@@ -468,7 +483,8 @@ cudaError_t wide_scatter(const PartitionCfg& pc, const FrontierView& in, u64 n_i
 
 template <int R>
 cudaError_t wide_merge(const PartitionCfg& pc, const void* regions, const u32* cursors, const FrontierView& out,
-                       unsigned n, bool write_out, StepScalars* sc, cudaStream_t stream) {
+                       unsigned n, bool write_out, const FrontierStepDev* next_step, StepScalars* sc,
+                       cudaStream_t stream) {
   if (pc.cap != (u32)kWCap) return cudaErrorInvalidValue;
   constexpr size_t smem = wide_merge_smem<R>();
   auto kern = wide_merge_kernel<R, kWBlock, kWH, kWCap>;
@@ -477,7 +493,8 @@ cudaError_t wide_merge(const PartitionCfg& pc, const void* regions, const u32* c
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, (u64)pc.sms * 2));
   kern<<<grid, kWBlock, smem, stream>>>(reinterpret_cast<const WCand<R>*>(regions), cursors,
                                         pc.cursor_stride ? pc.cursor_stride : 1, pc.parts,
-                                        reinterpret_cast<u128*>(out.keys), out.res, out.cap, n, write_out ? 1 : 0, sc);
+                                        reinterpret_cast<u128*>(out.keys), out.res, out.cap, n, write_out ? 1 : 0,
+                                        next_step, sc);
   return cudaGetLastError();
 }
 
@@ -500,13 +517,14 @@ cudaError_t launch_wide_partition_scatter(const PartitionCfg& pc, const Frontier
 
 cudaError_t launch_wide_partition_merge(const PartitionCfg& pc, const void* regions, const uint32_t* cursors,
                                         const FrontierView& out, unsigned n, bool write_out, StepScalars* sc,
-                                        cudaStream_t stream) {
+                                        cudaStream_t stream, const FrontierStepDev* next_step) {
   if (reinterpret_cast<uintptr_t>(regions) % 32) return cudaErrorInvalidValue;  // 256-bit candidate loads
+  if (n && next_step) return cudaErrorInvalidValue;                              // row keys or bond keys
   switch (pc.residues) {
-    case 1: return wide_merge<1>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 2: return wide_merge<2>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 3: return wide_merge<3>(pc, regions, cursors, out, n, write_out, sc, stream);
-    case 4: return wide_merge<4>(pc, regions, cursors, out, n, write_out, sc, stream);
+    case 1: return wide_merge<1>(pc, regions, cursors, out, n, write_out, next_step, sc, stream);
+    case 2: return wide_merge<2>(pc, regions, cursors, out, n, write_out, next_step, sc, stream);
+    case 3: return wide_merge<3>(pc, regions, cursors, out, n, write_out, next_step, sc, stream);
+    case 4: return wide_merge<4>(pc, regions, cursors, out, n, write_out, next_step, sc, stream);
   }
   return cudaErrorInvalidValue;
 }
