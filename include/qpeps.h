@@ -192,7 +192,8 @@ int qpeps_certify_c(const uint32_t* legs, const uint64_t* values, uint32_t len, 
 #define QPEPS_ORDER_TOP_LEFT_DIAMOND 1
 
 typedef struct qpeps_explicit_result {
-  uint32_t n, order, complete, pad0;
+  uint32_t n, order, complete;
+  uint32_t merge; /* the site steps' merge: QPEPS_MERGE_PARTITION (128-bit partitions) or QPEPS_MERGE_HASH */
   qpeps_u128 count;
   double elapsed_s;
   uint64_t peak_states, peak_open_bonds;

@@ -175,7 +175,7 @@ class ExplicitResult(ctypes.Structure):
         ("n", ctypes.c_uint32),
         ("order", ctypes.c_uint32),
         ("complete", ctypes.c_uint32),
-        ("pad0", ctypes.c_uint32),
+        ("merge", ctypes.c_uint32),
         ("count", U128),
         ("elapsed_s", ctypes.c_double),
         ("peak_states", ctypes.c_uint64),
@@ -516,6 +516,7 @@ class Context:
             "n": out.n,
             "order": out.order,
             "complete": bool(out.complete),
+            "merge": out.merge,
             "count": out.count.value if out.complete else None,
             "elapsed": out.elapsed_s,
             "peak_states": out.peak_states,

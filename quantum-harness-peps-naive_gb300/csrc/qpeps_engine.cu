@@ -1261,6 +1261,7 @@ struct ExplicitRun {
   double elapsed = 0, device_ms = 0;
   u64 peak_states = 1, peak_open_bonds = 0, contracted_sites = 0, launches = 0;
   u128 examined = 0, accepted = 0;
+  uint32_t merge = QPEPS_MERGE_PARTITION;
 };
 
 // One explicit-C frontier step through the 128-bit partitions, in place:
@@ -1490,6 +1491,7 @@ static void explicit_frontier(Ctx& ctx, unsigned n, unsigned order, u64 support_
   // The partitioned merge unless the tuning asks for the global table, or a
   // key could set all 128 bits (the partition tables' empty marker).
   const bool partitioned = ctx.tune.merge_auto != QPEPS_MERGE_HASH;
+  out.merge = partitioned ? QPEPS_MERGE_PARTITION : QPEPS_MERGE_HASH;
   FrontierStepDev* d_steps = nullptr;
   if (partitioned && total > 1) {
     buf_reserve(ctx, ctx.plan, total * sizeof(FrontierStepDev), p.budget, "explicit-C frontier steps");
@@ -2951,6 +2953,7 @@ int qpeps_explicit_frontier(void* ctx, uint32_t n, uint32_t order, uint64_t supp
     out->n = r.n;
     out->order = r.order;
     out->complete = r.complete ? 1 : 0;
+    out->merge = r.merge;
     out->count = to_abi(r.complete ? r.count : 0);
     out->elapsed_s = r.elapsed;
     out->peak_states = r.peak_states;

@@ -66,15 +66,18 @@ def test_range_and_argument_errors(ctx, qp):
 def test_partitioned_merge_equals_global_table(qp, order):
     """The explicit-C frontier through the 128-bit partitions (the default)
     and through the global table (merge_auto = MERGE_HASH) agree on every
-    field, complete and stopped at a support limit; the partitioned steps
-    launch a count, a scatter and a merge kernel."""
+    field, complete and stopped at a support limit. After its first step a
+    partitioned run launches a scatter and a merge per site (its merges count
+    the next step's matches), so it launches at most one kernel more than the
+    table's expand-insert and compaction."""
     part, table = qp.Context(0), qp.Context(0)
     try:
         table.set_tuning(merge_auto=qp.MERGE_HASH)
         for n in range(1, 13):
             a, b = part.explicit_frontier(n, order), table.explicit_frontier(n, order)
             assert {k: a[k] for k in FIELDS} == {k: b[k] for k in FIELDS}, n
-            assert a["gpu_launches"] > b["gpu_launches"]
+            assert a["merge"] == qp.MERGE_PARTITION and b["merge"] == qp.MERGE_HASH
+            assert a["gpu_launches"] <= b["gpu_launches"] + 1
         for limit in (50, 3000, 200_000):
             a, b = part.explicit_frontier(11, order, limit), table.explicit_frontier(11, order, limit)
             assert {k: a[k] for k in FIELDS} == {k: b[k] for k in FIELDS}, limit
