@@ -355,7 +355,9 @@ def run_ours(args):
     achieved = d["merge_kernel_bytes"] / max(d["device_ms"] / 1e3, 1e-12) / 1e9
     tuning = ctx.tuning
     kind = tuning.get("scatter_kind")
-    tpb = TRAFFIC_PER_ALGORITHMIC_BYTE.get(kind) if d["merge"] == 2 and args.grain == "row" else None
+    # The capture behind the factor is of the u64 row path's scatter and merge.
+    tpb = (TRAFFIC_PER_ALGORITHMIC_BYTE.get(kind)
+           if d["merge"] == 2 and args.grain == "row" and d["key_bits"] == 64 else None)
     roofline = {
         "bound": "hbm",
         "kernel": ("merge step: partition scatter + partition merge kernels" if d["merge"] == 2

@@ -252,7 +252,7 @@ constexpr size_t wide_merge_smem() {
 }
 
 template <int R, int BLOCK, int H, int CAP>
-__global__ void __launch_bounds__(BLOCK) wide_merge_kernel(const WCand<R>* __restrict__ regions,
+__global__ void __launch_bounds__(BLOCK, 2) wide_merge_kernel(const WCand<R>* __restrict__ regions,
                                                           const u32* __restrict__ cursors, u32 cstride, u32 parts,
                                                           u128* __restrict__ keys_out, u32* __restrict__ res_out,
                                                           u64 out_stride, unsigned n, int write_out,
