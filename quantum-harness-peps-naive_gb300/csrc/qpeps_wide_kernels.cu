@@ -251,8 +251,12 @@ constexpr size_t wide_merge_smem() {
   return (size_t)kWH * 16 + (size_t)R * kWH * 8 + (size_t)kWCap * 4;
 }
 
-template <int R, int BLOCK, int H, int CAP>
-__global__ void __launch_bounds__(BLOCK, 2) wide_merge_kernel(const WCand<R>* __restrict__ regions,
+// MINB: CTAs per SM the register allocation must allow. Row keys keep the
+// compiler's choice (one 512-thread CTA per SM at R = 2; capping it at two
+// measured slower); the explicit-C frontier's merge, which also matches the
+// next step's transitions, runs faster with two.
+template <int R, int BLOCK, int H, int CAP, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) wide_merge_kernel(const WCand<R>* __restrict__ regions,
                                                           const u32* __restrict__ cursors, u32 cstride, u32 parts,
                                                           u128* __restrict__ keys_out, u32* __restrict__ res_out,
                                                           u64 out_stride, unsigned n, int write_out,
@@ -487,7 +491,7 @@ cudaError_t wide_merge(const PartitionCfg& pc, const void* regions, const u32* c
                        cudaStream_t stream) {
   if (pc.cap != (u32)kWCap) return cudaErrorInvalidValue;
   constexpr size_t smem = wide_merge_smem<R>();
-  auto kern = wide_merge_kernel<R, kWBlock, kWH, kWCap>;
+  auto kern = next_step ? wide_merge_kernel<R, kWBlock, kWH, kWCap, 2> : wide_merge_kernel<R, kWBlock, kWH, kWCap, 1>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, (u64)pc.sms * 2));
