@@ -251,12 +251,13 @@ constexpr size_t wide_merge_smem() {
   return (size_t)kWH * 16 + (size_t)R * kWH * 8 + (size_t)kWCap * 4;
 }
 
-// MINB: CTAs per SM the register allocation must allow. Row keys keep the
-// compiler's choice (one 512-thread CTA per SM at R = 2; capping it at two
-// measured slower); the explicit-C frontier's merge, which also matches the
-// next step's transitions, runs faster with two.
-template <int R, int BLOCK, int H, int CAP, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) wide_merge_kernel(const WCand<R>* __restrict__ regions,
+// kBond: the explicit-C frontier's instantiation, which also matches the
+// written keys against the next site step's transitions (`next_step`); the
+// row-key one counts free columns at the next row instead (n > 0). Both are
+// held to two 512-thread CTAs per SM (64 registers): the row-key merge at one
+// CTA per SM ran 1.5x slower.
+template <int R, int BLOCK, int H, int CAP, bool kBond>
+__global__ void __launch_bounds__(BLOCK, 2) wide_merge_kernel(const WCand<R>* __restrict__ regions,
                                                           const u32* __restrict__ cursors, u32 cstride, u32 parts,
                                                           u128* __restrict__ keys_out, u32* __restrict__ res_out,
                                                           u64 out_stride, unsigned n, int write_out,
@@ -273,12 +274,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) wide_merge_kernel(const WCand<R>*
   __shared__ unsigned long long s_base;
   // Explicit-C frontier: the next site step's transitions, to count the
   // written boundary's matches there (its successor terms).
-  __shared__ u128 s_req_mask[kFrontierMaxTrans], s_req_value[kFrontierMaxTrans];
+  __shared__ u128 s_req_mask[kBond ? kFrontierMaxTrans : 1], s_req_value[kBond ? kFrontierMaxTrans : 1];
   __shared__ u32 s_next_trans;
   const int lane = threadIdx.x & 31;
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
-  const bool count_next = write_out && (n > 0 || next_step != nullptr);
-  if (next_step != nullptr) {
+  const bool count_next = write_out && (kBond ? next_step != nullptr : n > 0);
+  if constexpr (kBond) {
     if (threadIdx.x == 0) s_next_trans = min(next_step->n_trans, (u32)kFrontierMaxTrans);
     for (int t = threadIdx.x; t < kFrontierMaxTrans; t += BLOCK) {
       s_req_mask[t] = next_step->req_mask[t];
@@ -385,11 +386,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) wide_merge_kernel(const WCand<R>*
         kv.y = (u64)(key >> 64);
         reinterpret_cast<ulonglong2*>(keys_out)[idx] = kv;
       }
-      if (n) {
+      if constexpr (kBond) {
+        for (u32 t = 0; t < s_next_trans; ++t) nterms += (key & s_req_mask[t]) == s_req_value[t];
+      } else if (n) {
         const State st = unpack<u128>(key, n, mask);
         nterms += __popcll(~(st.cols | st.dr | st.dl) & mask);
-      } else if (next_step != nullptr) {
-        for (u32 t = 0; t < s_next_trans; ++t) nterms += (key & s_req_mask[t]) == s_req_value[t];
       }
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -491,7 +492,7 @@ cudaError_t wide_merge(const PartitionCfg& pc, const void* regions, const u32* c
                        cudaStream_t stream) {
   if (pc.cap != (u32)kWCap) return cudaErrorInvalidValue;
   constexpr size_t smem = wide_merge_smem<R>();
-  auto kern = next_step ? wide_merge_kernel<R, kWBlock, kWH, kWCap, 2> : wide_merge_kernel<R, kWBlock, kWH, kWCap, 1>;
+  auto kern = next_step ? wide_merge_kernel<R, kWBlock, kWH, kWCap, true> : wide_merge_kernel<R, kWBlock, kWH, kWCap, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, (u64)pc.sms * 2));
