@@ -1871,7 +1871,9 @@ static void graph_build(Ctx& ctx, unsigned n, const qpeps_options& o, const uint
             ok(launch_partition_scatter(st.pc, view, st.n_in, p.n, regions, cursors, sc, st_));
           }
           ok(cudaEventRecordWithFlags(g->ev[ei + 1], st_, cudaEventRecordExternal));
-          ok(launch_partition_merge(st.pc, regions, cursors, view, p.n, !st.final_step, sc, st_));
+          PartitionCfg mpc = st.pc;
+          mpc.count_next = 0;  // a replay's sizes are recorded: no next-row count
+          ok(launch_partition_merge(mpc, regions, cursors, view, p.n, !st.final_step, sc, st_));
           ok(cudaEventRecordWithFlags(g->ev[ei + 2], st_, cudaEventRecordExternal));
           ei += 3;
           g->launches += 2;

@@ -121,6 +121,7 @@ struct PartitionCfg {
                                   // 1 = CRT-folded residues, 2 = the planes hold an exact weight's
                                   // low and high words (both exact only when N! < p0 * p1, N <= 20)
   uint32_t key_bits = 64;         // 128: wide-key scatter and merge (32-byte candidates, `cap` = 1024)
+  uint32_t count_next = 1;        // fixed-layout row merges: count the next row's successor terms
   uint32_t scatter_block = 256;   // one-level scatters: threads per CTA (128, 256 or 512; 256 for R > 2)
   uint32_t merge_regs = 0;        // merge_kind 1, fixed layout: first claimants write their entries from
                                   // registers (no slot list in shared memory)

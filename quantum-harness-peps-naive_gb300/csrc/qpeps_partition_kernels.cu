@@ -514,6 +514,11 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   // buffer (read by the scatter, written here in place) stays intact for the
   // host's retry with smaller partitions.
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
+  // write_out: bit 0 writes the merged boundary, bit 1 also counts its
+  // successor terms at the next row (left out of CUDA-graph replays, whose
+  // sizes are recorded).
+  const bool count_next = (write_out & 2) != 0;
+  write_out &= 1;
   unsigned long long wsum[R], fsum[R], fstates = 0;
   unsigned long long nterms = 0;  // the written boundary's successor terms at the next row
   bool bad = false;  // an output index beyond the boundary buffer (skipped)
@@ -625,7 +630,8 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
         const bool wr = write_out && idx < out_stride;
         bad |= write_out && !wr;
         if (wr) keys_out[idx] = key;
-        if constexpr (!Layout::kSlotted) nterms += next_terms_of(L, key);
+        if constexpr (!Layout::kSlotted)
+          if (count_next) nterms += next_terms_of(L, key);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const u32 v = reduce_sum(s_acc[r * H + slot], r);
@@ -651,7 +657,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_kernel(const Cand<R>* _
   const unsigned long long t = pblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
   if constexpr (!Layout::kSlotted) {
-    if (write_out) {
+    if (write_out && count_next) {
       const unsigned long long nt = pblock_sum<BLOCK>(nterms);
       if (threadIdx.x == 0 && nt) atomicAdd(&sc->next_terms, nt);
       if (blockIdx.x == 0 && threadIdx.x == 0) sc->next_terms_ok = 1u;
@@ -733,6 +739,11 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   if constexpr (Layout::kSlotted)
     for (int i = threadIdx.x; i < (int)kServeMaxSlots * R; i += BLOCK) s_slot_fin[i] = 0ull;
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
+  // write_out: bit 0 writes the merged boundary, bit 1 also counts its
+  // successor terms at the next row (left out of CUDA-graph replays, whose
+  // sizes are recorded).
+  const bool count_next = (write_out & 2) != 0;
+  write_out &= 1;
   unsigned long long wsum[R], fsum[R], fstates = 0;
   // The written boundary's successor terms at the next row (the next row
   // step's count, so that it needs no counting pass of its own).
@@ -865,7 +876,8 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
           const bool wr = write_out && idx < out_stride;
           bad |= write_out && !wr;
           if (wr) keys_out[idx] = key;
-          if constexpr (kCountNext) nterms += next_terms_of(L, key);
+          if constexpr (kCountNext)
+            if (count_next) nterms += next_terms_of(L, key);
           const u64 folded = kFold ? s_acc[slot] : 0ull;
           if constexpr (kAcc == 2) {
             if (wr) {
@@ -898,7 +910,8 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
       const bool wr = write_out && idx < out_stride;
       bad |= write_out && !wr;
       if (wr) keys_out[idx] = key;
-      if constexpr (kCountNext) nterms += next_terms_of(L, key);
+      if constexpr (kCountNext)
+        if (count_next) nterms += next_terms_of(L, key);
       const u64 folded = kFold ? s_acc[slot] : 0ull;
       if constexpr (kAcc == 2) {
         if (wr) {
@@ -932,7 +945,7 @@ __global__ void __launch_bounds__(BLOCK) partition_merge_list_kernel(const Cand<
   const unsigned long long t = pblock_sum<BLOCK>(fstates);
   if (threadIdx.x == 0 && t) atomicAdd(&sc->final_states, t);
   if constexpr (kCountNext) {
-    if (write_out) {
+    if (write_out && count_next) {
       const unsigned long long nt = pblock_sum<BLOCK>(nterms);
       if (threadIdx.x == 0 && nt) atomicAdd(&sc->next_terms, nt);
       if (blockIdx.x == 0 && threadIdx.x == 0) sc->next_terms_ok = 1u;
@@ -1392,7 +1405,8 @@ cudaError_t merge_shape(const PartitionCfg& pc, int blocks_per_sm, const void* r
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, capb));
   kern<<<grid, BLOCK, smem, stream>>>(reinterpret_cast<const Cand<R>*>(regions), cursors,
                                       pc.cursor_stride ? pc.cursor_stride : 1, pc.parts,
-                                      reinterpret_cast<u64*>(out.keys), out.res, out.cap, L, write_out ? 1 : 0, sc);
+                                      reinterpret_cast<u64*>(out.keys), out.res, out.cap, L,
+                                      (write_out ? 1 : 0) | (pc.count_next ? 2 : 0), sc);
   return cudaGetLastError();
 }
 

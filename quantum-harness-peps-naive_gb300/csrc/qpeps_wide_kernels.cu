@@ -278,7 +278,10 @@ __global__ void __launch_bounds__(BLOCK, 2) wide_merge_kernel(const WCand<R>* __
   __shared__ u32 s_next_trans;
   const int lane = threadIdx.x & 31;
   if (*reinterpret_cast<volatile const u32*>(&sc->error)) return;
-  const bool count_next = write_out && (kBond ? next_step != nullptr : n > 0);
+  // write_out: bit 0 writes the merged boundary, bit 1 lets the row-key
+  // merge count its successor terms at the next row.
+  const bool count_next = (write_out & 1) && (kBond ? next_step != nullptr : (n > 0 && (write_out & 2)));
+  write_out &= 1;
   if constexpr (kBond) {
     if (threadIdx.x == 0) s_next_trans = min(next_step->n_trans, (u32)kFrontierMaxTrans);
     for (int t = threadIdx.x; t < kFrontierMaxTrans; t += BLOCK) {
@@ -498,8 +501,8 @@ cudaError_t wide_merge(const PartitionCfg& pc, const void* regions, const u32* c
   const unsigned grid = (unsigned)std::max<u64>(1, std::min<u64>(pc.parts, (u64)pc.sms * 2));
   kern<<<grid, kWBlock, smem, stream>>>(reinterpret_cast<const WCand<R>*>(regions), cursors,
                                         pc.cursor_stride ? pc.cursor_stride : 1, pc.parts,
-                                        reinterpret_cast<u128*>(out.keys), out.res, out.cap, n, write_out ? 1 : 0,
-                                        next_step, sc);
+                                        reinterpret_cast<u128*>(out.keys), out.res, out.cap, n,
+                                        (write_out ? 1 : 0) | (pc.count_next ? 2 : 0), next_step, sc);
   return cudaGetLastError();
 }
 
