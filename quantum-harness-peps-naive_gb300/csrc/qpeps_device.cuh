@@ -2,7 +2,8 @@
 //
 // Boundary key layout (row granularity) is the reference's PackedBoundary
 // (src/lib.rs:348-377): bits [0,n) columns, [n,2n) diag_dr, [2n,3n) diag_dl.
-// A key is held in `uint64_t` when 3n <= 63 (N <= 21) and in
+// A key is held in `uint64_t` up to N = 22 (the reference layout up to 21, a
+// compact layout of the 3n - 2 live bits at 22, see pack/unpack) and in
 // `unsigned __int128` otherwise (N <= 42). Mid-row (site granularity) keys
 // add the row signal at bit 3n; the u64 form is used for N <= 20 there.
 //
